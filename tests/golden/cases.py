@@ -1,0 +1,133 @@
+"""Inputs of the golden fixtures and of the parity tests.
+
+The small cases follow the shapes of the reference harness's batch-path
+scenarios (qdt_verify.cpp: `structured` :1033-1163, `batch` :1165-1190,
+`magnitudes` :1192-1231, `scale` :1233-1258, `circle` :1260-1298, and the
+example inputs :745-787), generated here with numpy seeds of our own. The
+large specs are the workloads of the benchmark and the reference README's
+known-answer sizes.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from libqdt_gb300 import workloads as W
+
+
+def _structured():
+    out = []
+    g = [(i, j) for i in range(40) for j in range(40)]
+    out.append(("grid40", g))
+    out.append(("collinear_diagonal", [(i, 2 * i) for i in range(50)]))
+    out.append(("collinear_horizontal", [(i, 7) for i in range(50)]))
+    out.append(("collinear_vertical", [(7, i) for i in range(50)]))
+    out.append(("line_plus_one", [(i, 7) for i in range(50)] + [(25, 8)]))
+    out.append(("parabola", [(i, i * i) for i in range(30)]))
+    out.append(("all_duplicates", [(5, 5)] * 100))
+    r = 1 << 27
+    out.append(("near_circle_2p27", [(int(np.round(r * np.cos(2 * np.pi * i / 200))),
+                                      int(np.round(r * np.sin(2 * np.pi * i / 200)))) for i in range(200)]))
+    out.append(("two_rows", [p for i in range(100) for p in ((i, 0), (i, 1))]))
+    out.append(("triangle_with_duplicates", [p for _ in range(20) for p in ((0, 0), (1, 0), (0, 1))]))
+    out.append(("empty", []))
+    out.append(("one_point", [(1, 1)]))
+    out.append(("two_points", [(1, 1), (2, 3)]))
+    out.append(("three_collinear", [(0, 0), (1, 1), (2, 2)]))
+    out.append(("three_points", [(0, 0), (5, 0), (0, 5)]))
+    m = 1 << 28
+    out.append(("coords_2p28", [(-m, -m), (m, -m), (0, m), (1, 1), (-1, 2)]))
+    out.append(("square4", [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0), (1.0, 1.0)]))
+    out.append(("quad", [(0.0, 0.0), (4.0, 0.0), (3.0, 1.0), (1.0, 1.0)]))
+    return out
+
+
+def small_cases():
+    """(name, (n, 2) float64 array) pairs, each a few thousand points at most."""
+    cases = []
+    for name, pts in _structured():
+        base = np.array(pts, dtype=np.float64).reshape(-1, 2)
+        for s in range(5):
+            p = base.copy()
+            if s:
+                p = p[np.random.default_rng(77 + s).permutation(p.shape[0])]
+            cases.append(("%s_s%d" % (name, s), p))
+
+    ranges = [2, 3, 4, 6, 10, 30, 100, 10000, 1 << 20]
+    for s in range(40):
+        rng = np.random.default_rng(1000 + s)
+        n = int(rng.integers(0, 70))
+        R = ranges[int(rng.integers(0, len(ranges)))]
+        cases.append(("batch_%d" % s, rng.integers(-R, R + 1, size=(n, 2)).astype(np.float64)))
+
+    levels = [0, 2, 5, 9, 14, 20, 26, 28]
+    for s in range(30):
+        rng = np.random.default_rng(41000 + s)
+        mode = s % 3
+        n = 4 + int(rng.integers(0, 60))
+        offx = (1 if rng.integers(0, 2) else -1) * (1 << 27)
+        offy = (1 if rng.integers(0, 2) else -1) * (1 << 27)
+        pts = []
+        for i in range(n):
+            far = mode == 1 or (mode == 2 and (i & 1))
+            if far:
+                b = 1 << int(rng.integers(0, 9))
+                pts.append((offx + int(rng.integers(-b, b + 1)), offy + int(rng.integers(-b, b + 1))))
+            else:
+                b = 1 << levels[int(rng.integers(0, len(levels)))]
+                pts.append((int(rng.integers(-b, b + 1)), int(rng.integers(-b, b + 1))))
+        cases.append(("magnitudes_%d" % s, np.array(pts, dtype=np.float64)))
+
+    for k in (-1000, -600, -300, -64, 64, 300, 600, 900):
+        for s in range(6):
+            rng = np.random.default_rng(31000 + s)
+            R = 6 if rng.integers(0, 2) else 1000
+            n = 3 + int(rng.integers(0, 40))
+            p = rng.integers(-R, R + 1, size=(n, 2)).astype(np.float64) * np.ldexp(1.0, k)
+            cases.append(("scale_%d_%d" % (k, s), p))
+
+    for s in range(20):
+        rng = np.random.default_rng(55000 + s)
+        n = 8 + int(rng.integers(0, 120))
+        Rr = 1 << (20 + int(rng.integers(0, 8)))
+        a = 2 * np.pi * rng.integers(0, 100000, size=n) / 100000.0
+        cases.append(("circle_%d" % s, np.stack([np.round(Rr * np.cos(a)), np.round(Rr * np.sin(a))], axis=1)))
+
+    cases.append(("uniform_2000", W.uniform(2000, 101)))
+    cases.append(("lattice_32_dups", W.lattice_with_duplicates(32, 0.05, 102)))
+    cases.append(("gauss_2000", W.gaussian_mixture(2000, 8, 103)))
+    cases.append(("unit_circle_500", W.unit_circle(500, 104)))
+    cases.append(("noisy_line_1000", W.noisy_line(1000, 105)))
+    cases.append(("bench_uniform_100", W.bench_uniform(100, W.BENCH_SEED + 100)))
+    return cases
+
+
+def large_specs():
+    specs = []
+    for n in sorted(W.BENCH_KNOWN_COUNTS):
+        specs.append({"name": "bench_uniform_%d" % n, "gen": "bench_uniform", "n": n,
+                      "seed": W.BENCH_SEED + n, "known_ntri": W.BENCH_KNOWN_COUNTS[n]})
+    specs.append({"name": "uniform_100k", "gen": "uniform", "n": 100000, "seed": 12345})
+    specs.append({"name": "uniform_1m", "gen": "uniform", "n": 1048576, "seed": 1})
+    specs.append({"name": "uniform_2p6m", "gen": "uniform", "n": 2600000, "seed": 2})
+    specs.append({"name": "lattice_1024_dups", "gen": "lattice", "n": 1024, "seed": 7})
+    specs.append({"name": "gauss_4m", "gen": "gauss", "n": 4000000, "seed": 11})
+    specs.append({"name": "circle_100k", "gen": "circle", "n": 100000, "seed": 13})
+    specs.append({"name": "line_1m", "gen": "line", "n": 1000000, "seed": 17})
+    return specs
+
+
+def make_large(spec) -> np.ndarray:
+    g = spec["gen"]
+    if g == "bench_uniform":
+        return W.bench_uniform(spec["n"], spec["seed"])
+    if g == "uniform":
+        return W.uniform(spec["n"], spec["seed"])
+    if g == "lattice":
+        return W.lattice_with_duplicates(spec["n"], 0.01, spec["seed"])
+    if g == "gauss":
+        return W.gaussian_mixture(spec["n"], 64, spec["seed"])
+    if g == "circle":
+        return W.unit_circle(spec["n"], spec["seed"])
+    if g == "line":
+        return W.noisy_line(spec["n"], spec["seed"])
+    raise ValueError(g)

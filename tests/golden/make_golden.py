@@ -1,0 +1,113 @@
+"""Generates the golden fixtures of the batch path from the reference itself.
+
+Run in a container that has the reference tree (it is compiled from its own
+sources into oracle/_ref by oracle/build_ref.sh):
+
+    python tests/golden/make_golden.py
+
+It feeds seeded inputs to the reference library through its C ABI
+(qdt_execute and qdt_execute_parallel), reads the triangles back with
+qdt_get_triangle and the used-point flags with qdt_point_is_used, and
+writes:
+
+* small_cases.npz -- points, canonical triangles and used flags of small
+  structured and random cases (full arrays);
+* digests.json    -- for the large workloads: counts and SHA-256 digests of
+  the canonical triangle list and of the used flags.
+
+The canonical form is the reference harness's (qdt_verify.cpp:408-427).
+Nothing at test time reads the reference; the tests read only these files.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from libqdt_gb300 import qdt_api as Q  # noqa: E402
+from libqdt_gb300 import workloads as W  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests.golden import cases as C  # noqa: E402
+
+
+_dump = None
+
+
+def run_ref(lib, pts, parallel):
+    """Runs the reference's batch call and reads the context back through its
+    query functions (in bulk, via oracle/qdt_dump.c)."""
+    global _dump
+    import ctypes
+    if _dump is None:
+        _dump = ctypes.CDLL(os.path.join(O.REF_DIR, "libqdt_dump_ref.so"))
+        _dump.qdt_dump_triangles.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        _dump.qdt_dump_triangles.restype = ctypes.c_size_t
+        _dump.qdt_dump_used.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        _dump.qdt_dump_used.restype = ctypes.c_size_t
+    with Q.Context(lib) as c:
+        st = c.execute(pts, parallel=parallel)
+        tris = np.zeros((c.triangles_size(), 3), dtype=np.int64)
+        used = np.zeros(c.points_size(), dtype=np.uint8)
+        _dump.qdt_dump_triangles(c.ptr, tris.ctypes.data)
+        _dump.qdt_dump_used(c.ptr, used.ctypes.data)
+    return st, tris, used
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def main():
+    if not O.build_reference():
+        print("reference not available; nothing generated")
+        return 1
+    lib = Q.load(O.REF_LIB_PATH)
+
+    small = {}
+    for name, pts in C.small_cases():
+        st, tris, used = run_ref(lib, pts, False)
+        st2, tris2, used2 = run_ref(lib, pts, True)
+        ct = O.canonical(tris)
+        assert st == 0 and st2 == 0, name
+        assert np.array_equal(ct, O.canonical(tris2)), name
+        assert np.array_equal(used, used2), name
+        small[name + "/pts"] = pts
+        small[name + "/tris"] = ct.astype(np.int64)
+        small[name + "/used"] = used
+    np.savez_compressed(os.path.join(HERE, "small_cases.npz"), **small)
+    print("small cases:", len(small) // 3)
+
+    out = {"canonical_form": "qdt_verify.cpp:408-427", "cases": []}
+    for spec in C.large_specs():
+        pts = C.make_large(spec)
+        rec = dict(spec)
+        for par in (False, True):
+            t0 = time.time()
+            st, tris, used = run_ref(lib, pts, par)
+            ct = O.canonical(tris)
+            key = "threaded" if par else "serial"
+            rec[key] = {
+                "status": int(st),
+                "ntri": int(ct.shape[0]),
+                "tri_digest": digest(ct.astype(np.int64)),
+                "used_digest": digest(used),
+                "used_count": int(used.sum()),
+            }
+            print(spec["name"], key, ct.shape[0], "%.1fs" % (time.time() - t0), flush=True)
+        rec["npts"] = int(pts.shape[0])
+        out["cases"].append(rec)
+    with open(os.path.join(HERE, "digests.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
