@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Benchmark of the batch Delaunay triangulation path.
+
+Metric: Mpoints/s triangulated, with 0 exact-predicate violations (checked
+once per run, outside the timed region, by the oracle's exact checker).
+Workload (default): 2,600,000 float64 points uniform in [0,1)^2 -- the
+single-GPU plain-path configuration the target is quoted on. Data are
+synthetic (seeded), as the reference's own benchmark is.
+
+GB300 arm (default):
+  value -- device-resident: the points are in HBM when the timed region
+           starts; one step = qdtg_execute_device() (all stages, result in
+           HBM). Timed with CUDA events on the library's stream; L2 flushed
+           (256 MiB write) between steps, outside the events.
+  e2e   -- through qdt_execute() with host buffers: host copy into the
+           context, H2D, all stages, D2H of triangles and representatives;
+           wall-clock per call.
+Reference arm (--impl reference): the CPU restatement of the reference's
+threaded batch driver (oracle/, pthreads, all host cores) on the same
+workload -- the reference's own sources are not available on this machine.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path has no exchange step); value = all ranks' points / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpoints/s triangulated (0 exact violations), single+batched; p50/p99 latency"
+UNIT = "Mpoints/s"
+
+WORKLOADS = {
+    "uniform_2p6m": ("uniform", 2600000, 2),
+    "uniform_1m": ("uniform", 1048576, 1),
+    "lattice_1024_dups": ("lattice", 1024, 7),
+    "gauss_4m": ("gauss", 4000000, 11),
+    "uniform_100k": ("uniform", 100000, 12345),
+}
+
+
+def make_points(name):
+    from libqdt_gb300 import workloads as W
+    kind, n, seed = WORKLOADS[name]
+    if kind == "uniform":
+        return W.uniform(n, seed)
+    if kind == "lattice":
+        return W.lattice_with_duplicates(n, 0.01, seed)
+    if kind == "gauss":
+        return W.gaussian_mixture(n, 64, seed)
+    raise ValueError(name)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", "qdt_clocks_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out["sm_mhz"] = statistics.median(sm)
+            out["sm_max_mhz"] = max(mx)
+            out["samples"] = len(sm)
+        out["reasons"] = sorted(reasons)
+        return out
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_threads():
+    return max(1, min(64, os.cpu_count() or 1))
+
+
+def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's threaded
+    batch driver, all host threads, on the same workload."""
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    pts = make_points(args.workload)
+    n = pts.shape[0]
+    nt = cpu_threads()
+    for _ in range(args.warmup):
+        O.triangulate(pts, threaded=True, nthreads=nt)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = O.triangulate(pts, threaded=True, nthreads=nt)
+        times.append(time.perf_counter() - t0)
+        assert r.status == 0
+    ms = 1e3 * statistics.mean(times)
+    value = n / (ms / 1e3) / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "points": n, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nt, "kind": "port",
+                         "sample": "full workload (%d points) per step, threaded driver" % n},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    import libqdt_gb300 as G
+    from oracle import delaunay_check as D
+    from oracle import oracle as O
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    pts = make_points(args.workload)
+    n = pts.shape[0]
+    lib = G.load()
+    t = G.Triangulation(lib)
+    t.set_options(count_filter_failures=False, stage_timing=True)
+    d_pts = torch.from_numpy(pts).cuda().contiguous()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    # correctness once, outside the timed region: exact checker on the result
+    st = t.execute_device(d_pts.data_ptr(), n)
+    if st != 0:
+        raise RuntimeError("qdtg_execute_device failed: %d" % st)
+    tris = t.download_device_triangles()
+    viol = None
+    if not args.no_check:
+        rep = O.triangulate(pts).rep if n <= 4_000_000 else None
+        res = D.check(pts, tris, rep)
+        viol = int(sum(res.values()))
+    ntri = tris.shape[0]
+    m = t.run_info()["unique_points"]
+
+    stream = torch.cuda.ExternalStream(t.stream())
+    for _ in range(max(0, args.warmup - 1)):
+        t.execute_device(d_pts.data_ptr(), n)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, stage = [], {}
+    launches = 0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = t.execute_device(d_pts.data_ptr(), n)
+        e1.record(stream)
+        e1.synchronize()
+        if st != 0:
+            raise RuntimeError("qdtg_execute_device failed: %d" % st)
+        step_ms.append(e0.elapsed_time(e1))
+        info = t.run_info()
+        launches += info["kernel_launches"]
+        for k in ("ms_sort", "ms_unique", "ms_split", "ms_build", "ms_extract"):
+            stage.setdefault(k, []).append(info[k])
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ck = clocks.stop()
+    ms = statistics.mean(step_ms)
+    if dist:
+        x = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        ms = float(x.item())
+    value = ws * n / (ms / 1e3) / 1e6
+
+    # end to end through qdt_execute with host buffers
+    e2e_ms = []
+    for _ in range(max(1, args.warmup)):
+        t.execute(pts)
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = t.execute(pts)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+        if st != 0:
+            raise RuntimeError("qdt_execute failed: %d" % st)
+    e2e = statistics.mean(e2e_ms)
+    if dist:
+        x = torch.tensor([e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        e2e = float(x.item())
+    e2e_value = ws * n / (e2e / 1e3) / 1e6
+    h2d = 16 * n
+    d2h = 4 * 3 * 2 * m + 4 * n + 64
+
+    # roofline of the dominant stage
+    stage_ms = {k: statistics.mean(v) for k, v in stage.items()}
+    peak, peak_kind = peaks()
+    # algorithmic bytes per point of each stage ("Roofline")
+    nrec = 3 * m
+    alg = {
+        "ms_sort": 16 * n + 20 * n + 16 * (16 * n + 40 * n),   # keys + 16 radix passes (hist read, scatter r+w)
+        "ms_unique": 16 * n + 4 * n + 16 * m + 8 * m + 4 * n,
+        "ms_split": 0,
+        "ms_build": 16 * m + 32 * nrec,
+        "ms_extract": 32 * nrec + 12 * ntri,
+    }
+    top = max(stage_ms, key=lambda k: stage_ms[k])
+    achieved = (alg[top] or 1) / (stage_ms[top] / 1e3) / 1e9 if stage_ms[top] > 0 else 0.0
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform [0,1)^2)",
+        "config": {"workload": args.workload, "points": n, "distinct": m, "triangles": ntri,
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "single"},
+        "exact_violations": viol,
+        "stage_ms": {k[3:]: round(v, 4) for k, v in stage_ms.items()},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(e2e, 3)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "stage": top[3:], "achieved": round(achieved, 2), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 5),
+                     "traffic": None, "algorithmic_bytes": alg[top]},
+        "clocks": ck,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        nt = cpu_threads()
+        times = []
+        t0 = time.perf_counter()
+        while len(times) < 5 and time.perf_counter() - t0 < 20:
+            a = time.perf_counter()
+            O.triangulate(pts, threaded=True, nthreads=nt)
+            times.append(time.perf_counter() - a)
+        cb = n / statistics.median(times) / 1e6
+        line["cpu_baseline"] = {"value": round(cb, 4), "unit": UNIT, "cores": nt, "kind": "port",
+                                "sample": "%d full runs of the workload, threaded driver" % len(times)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    t.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="uniform_2p6m", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

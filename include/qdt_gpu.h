@@ -1,0 +1,90 @@
+/*
+ * qdt_gpu.h -- GPU-specific additions to the qdt.h interface.
+ *
+ * qdt.h is the drop-in boundary and stays as the reference has it. The
+ * functions here are additive: they have no counterpart in the reference and
+ * expose what only a GPU implementation can offer -- input that already lives
+ * in device memory, results read in bulk instead of one triangle per call,
+ * per-stage timing, and the filter-failure counters of the exact predicates.
+ */
+#if !defined(_LIB_QDT_GPU_H_)
+#define _LIB_QDT_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "qdt.h"
+
+#if __cplusplus
+extern "C"
+{
+#endif
+
+/* What the last batch call of a context did. Times are milliseconds measured
+   with CUDA events on the context's stream (0 unless timing is enabled with
+   qdtg_set_options). */
+typedef struct qdtg_run_info
+{
+    size_t             n;               /* input points */
+    size_t             unique_points;   /* distinct points */
+    size_t             triangles;
+    unsigned long long orient_exact;    /* orient2d calls that needed the exact path (if counted) */
+    unsigned long long incircle_exact;  /* in-circle calls that needed the exact path (if counted) */
+    float              ms_h2d, ms_sort, ms_unique, ms_split, ms_build, ms_extract, ms_d2h, ms_total;
+    int                device_flags;    /* device status bits; 0 = clean */
+    int                kernel_launches; /* kernels the call launched */
+} qdtg_run_info;
+
+/* Options of a context: count_filter_failures != 0 counts the predicate calls
+   that fall back to exact arithmetic (adds atomics on that rare path);
+   stage_timing != 0 records CUDA events between the stages. */
+QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_timing);
+
+/* Fills *info for the last batch call of the context. Returns 1, or 0 when
+   ptr or info is NULL. */
+QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info);
+
+/* Batch triangulation of n points that are already in device memory (d_pts,
+   16-byte aligned for the fastest path). The work is ordered after the work
+   already queued on cuda_stream (a cudaStream_t; NULL for none) and the call
+   returns when it is done. The triangles stay in device memory:
+   qdtg_device_triangles() gives them. The host side of the context is left
+   empty (no points, no triangles), as after a rejected batch call. Input
+   checks and status codes are those of qdt_execute(). */
+QDT_API qdt_status qdtg_execute_device(qdt_t* ptr, const qdt_vec2d* d_pts, size_t n, void* cuda_stream);
+
+/* After qdtg_execute_device(): the number of triangles, and in *d_tris (if
+   not NULL) a device pointer to 3 * count uint32 point indices, valid until
+   the next batch call or qdt_destroy(). */
+QDT_API size_t qdtg_device_triangles(const qdt_t* ptr, const uint32_t** d_tris);
+
+/* After qdtg_execute_device(): copies min(cap, count) device triangles (3
+   indices each) to host memory out and returns how many. */
+QDT_API size_t qdtg_download_device_triangles(const qdt_t* ptr, uint32_t* out, size_t cap);
+
+/* Bulk copies of the host results of the last batch call (or of the current
+   triangulation after insertions and constraints). qdtg_copy_triangles
+   writes min(cap, qdt_triangles_size) triangles (3 indices each) and returns
+   how many; qdtg_copy_rep writes min(cap, qdt_points_size) representatives
+   (the lowest index with the same coordinates) and returns how many. */
+QDT_API size_t qdtg_copy_triangles(const qdt_t* ptr, uint32_t* out, size_t cap);
+QDT_API size_t qdtg_copy_rep(const qdt_t* ptr, uint32_t* out, size_t cap);
+
+/* The CUDA stream (a cudaStream_t) on which the context's GPU work runs;
+   NULL before the context's first batch call. Lets a caller order its own
+   work or time the calls with CUDA events on that stream. */
+QDT_API void* qdtg_stream(const qdt_t* ptr);
+
+/* The CUDA error code of the last failed GPU call of the context (0 if
+   none), e.g. when qdt_execute() returned QDT_ERR_INTERNAL because no GPU is
+   present. */
+QDT_API int qdtg_last_cuda_error(const qdt_t* ptr);
+
+/* Library version string. */
+QDT_API const char* qdtg_version(void);
+
+#if __cplusplus
+}
+#endif
+
+#endif

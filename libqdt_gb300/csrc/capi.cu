@@ -1,0 +1,443 @@
+// The C interface (include/qdt.h, include/qdt_gpu.h): input checks, status
+// codes, reset-on-failure, queries. Mirrors the reference shim
+// (libqdt/qdt.cpp) function by function; no C++ exception crosses it.
+#include <cmath>
+#include <new>
+
+#include "context.hpp"
+#include "qdt.h"
+#include "qdt_gpu.h"
+
+using qdtg::Context;
+
+namespace qdtg {
+
+void Context::reset() noexcept
+{
+    points.clear();
+    rep.clear();
+    tris.clear();
+    unique_points = 0;
+    if (mesh)
+    {
+        mesh_destroy(mesh);
+        mesh = nullptr;
+    }
+}
+
+void Context::reset_release() noexcept
+{
+    reset();
+    PinnedVec<double>().swap(points);
+    PinnedVec<uint32_t>().swap(rep);
+    PinnedVec<uint32_t>().swap(tris);
+}
+
+Context::~Context()
+{
+    if (mesh) mesh_destroy(mesh);
+    delete engine;
+}
+
+static int ensure_engine(Context& c)
+{
+    if (c.engine) return QDT_OK;
+    int err = 0;
+    c.engine = Engine::create(&err);
+    if (!c.engine)
+    {
+        c.last_cuda_error = err ? err : -1;
+        return QDT_ERR_INTERNAL;
+    }
+    return QDT_OK;
+}
+
+int rebuild_from_points(Context& c)
+{
+    const int e = ensure_engine(c);
+    if (e != QDT_OK) return e;
+    // the engine reads from the caller's array while it fills `points`:
+    // hand it a separate copy
+    PinnedVec<double> src(c.points);
+    size_t            ntri = 0, uniq = 0;
+    const int         st = c.engine->run_host(src.data(), src.size() / 2, c.points, c.tris, &ntri, c.rep, &uniq);
+    if (st != QDT_OK) return st;
+    c.unique_points = uniq;
+    if (c.mesh)
+    {
+        mesh_destroy(c.mesh);
+        c.mesh = nullptr;
+    }
+    return QDT_OK;
+}
+
+}  // namespace qdtg
+
+namespace {
+
+inline Context* ctx(qdt_t* p) { return reinterpret_cast<Context*>(p); }
+inline const Context* ctx(const qdt_t* p) { return reinterpret_cast<const Context*>(p); }
+
+inline bool point_ok(double x, double y) { return std::isfinite(x) && std::isfinite(y); }
+
+// reference qdt.cpp:63-77
+qdt_status status_from_current_exception() noexcept
+{
+    try
+    {
+        throw;
+    }
+    catch (const std::bad_alloc&)
+    {
+        return QDT_ERR_OUT_OF_MEMORY;
+    }
+    catch (...)
+    {
+        return QDT_ERR_INTERNAL;
+    }
+}
+
+void fill_results(qdt_status* results, size_t n, qdt_status st) noexcept
+{
+    if (!results) return;
+    for (size_t i = 0; i < n; ++i) results[i] = st;
+}
+
+// reference qdt.cpp:29-43 and :88-113. The finiteness scan of the input runs
+// on the GPU, fused into the key transform (same order of checks: the count
+// and NULL are tested first, on the host).
+qdt_status execute_impl(qdt_t* ptr, const qdt_vec2d* pts, size_t n)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    try
+    {
+        if (n > qdtg::kMaxPoints)
+        {
+            c->reset();
+            return QDT_ERR_TOO_MANY_POINTS;
+        }
+        if (n > 0 && !pts)
+        {
+            c->reset();
+            return QDT_ERR_NULL_ARGUMENT;
+        }
+        c->reset();
+        if (n == 0) return QDT_OK;
+        int st = qdtg::ensure_engine(*c);
+        if (st != QDT_OK)
+        {
+            c->reset();
+            return (qdt_status)st;
+        }
+        size_t ntri = 0, uniq = 0;
+        st = c->engine->run_host(reinterpret_cast<const double*>(pts), n, c->points, c->tris, &ntri, c->rep, &uniq);
+        if (st != QDT_OK)
+        {
+            c->reset();
+            return (qdt_status)st;
+        }
+        c->unique_points = uniq;
+        return QDT_OK;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        return st;
+    }
+}
+
+// reference qdt.cpp:116-142
+qdt_status insert_point_impl(qdt_t* ptr, const qdt_vec2d& pt, size_t* index, bool parallel)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    try
+    {
+        if (!point_ok(pt.x, pt.y)) return QDT_ERR_NOT_FINITE;
+        if (c->npoints() >= qdtg::kMaxPoints) return QDT_ERR_TOO_MANY_POINTS;
+        const int st = qdtg::mesh_insert_point(*c, pt.x, pt.y, parallel);
+        if (st != QDT_OK)
+        {
+            c->reset();
+            return (qdt_status)st;
+        }
+        if (index) *index = c->npoints() - 1;
+        return QDT_OK;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        return st;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+QDT_API const char* qdt_status_string(qdt_status status)
+{
+    switch (status)
+    {
+    case QDT_OK: return "success";
+    case QDT_ERR_NULL_CONTEXT: return "the context is NULL";
+    case QDT_ERR_NULL_ARGUMENT: return "a required pointer argument is NULL";
+    case QDT_ERR_TOO_MANY_POINTS: return "more than 100000000 points";
+    case QDT_ERR_NOT_FINITE: return "a coordinate is NaN or infinite";
+    case QDT_ERR_INVALID_INDEX: return "an end point index is not a point of the context";
+    case QDT_ERR_SAME_POINT: return "both end points are the same point";
+    case QDT_ERR_NO_TRIANGLES: return "the context has no triangles";
+    case QDT_ERR_CROSSES_CONSTRAINT: return "the segment crosses an existing constraint";
+    case QDT_ERR_THROUGH_POINT: return "the segment passes through another point";
+    case QDT_ERR_OUT_OF_MEMORY: return "out of memory";
+    case QDT_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+QDT_API qdt_t* qdt_create(void) { return reinterpret_cast<qdt_t*>(new (std::nothrow) Context()); }
+
+QDT_API qdt_status qdt_execute(qdt_t* ptr, const qdt_vec2d* pts, size_t n) { return execute_impl(ptr, pts, n); }
+
+QDT_API qdt_status qdt_execute_parallel(qdt_t* ptr, const qdt_vec2d* pts, size_t n)
+{
+    return execute_impl(ptr, pts, n);
+}
+
+QDT_API qdt_status qdt_insert_point(qdt_t* ptr, qdt_vec2d pt, size_t* index)
+{
+    return insert_point_impl(ptr, pt, index, false);
+}
+
+QDT_API qdt_status qdt_insert_point_parallel(qdt_t* ptr, qdt_vec2d pt, size_t* index)
+{
+    return insert_point_impl(ptr, pt, index, true);
+}
+
+// reference qdt.cpp:193-212
+QDT_API qdt_status qdt_insert_constraint(qdt_t* ptr, size_t v0, size_t v1)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    try
+    {
+        const qdt_status st = (qdt_status)qdtg::mesh_insert_constraint(*c, v0, v1);
+        if (st == QDT_ERR_INTERNAL) c->reset();
+        return st;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        return st;
+    }
+}
+
+// reference qdt.cpp:214-244 with Wrapper.cpp:1264-1285
+QDT_API qdt_status qdt_insert_constraints_batch(qdt_t* ptr, const qdt_edge* edges, size_t num_edges,
+    qdt_status* results)
+{
+    Context* c = ctx(ptr);
+    if (!c)
+    {
+        fill_results(results, num_edges, QDT_ERR_NULL_CONTEXT);
+        return QDT_ERR_NULL_CONTEXT;
+    }
+    if (num_edges == 0) return QDT_OK;
+    if (!edges)
+    {
+        fill_results(results, num_edges, QDT_ERR_NULL_ARGUMENT);
+        return QDT_ERR_NULL_ARGUMENT;
+    }
+    try
+    {
+        qdt_status first = QDT_OK;
+        for (size_t i = 0; i < num_edges; ++i)
+        {
+            const qdt_status st = (qdt_status)qdtg::mesh_insert_constraint(*c, edges[i].v0, edges[i].v1);
+            if (st == QDT_ERR_INTERNAL)
+            {
+                c->reset();
+                fill_results(results, num_edges, QDT_ERR_INTERNAL);
+                return QDT_ERR_INTERNAL;
+            }
+            if (results) results[i] = st;
+            if (st != QDT_OK && first == QDT_OK) first = st;
+        }
+        return first;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        fill_results(results, num_edges, st);
+        return st;
+    }
+}
+
+QDT_API size_t qdt_triangles_size(const qdt_t* ptr)
+{
+    const Context* c = ctx(ptr);
+    return c ? c->ntris() : 0;
+}
+
+QDT_API size_t qdt_get_triangle(const qdt_t* ptr, size_t T[3], size_t id)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !T) return 0;
+    if (id >= c->ntris()) return 0;
+    const uint32_t* t = c->tris.data() + 3 * id;
+    T[0] = t[0];
+    T[1] = t[1];
+    T[2] = t[2];
+    return 1;
+}
+
+QDT_API size_t qdt_points_size(const qdt_t* ptr)
+{
+    const Context* c = ctx(ptr);
+    return c ? c->npoints() : 0;
+}
+
+QDT_API size_t qdt_get_point(const qdt_t* ptr, qdt_vec2d* pt, size_t id)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !pt) return 0;
+    if (id >= c->npoints()) return 0;
+    pt->x = c->points[2 * id];
+    pt->y = c->points[2 * id + 1];
+    return 1;
+}
+
+// reference qdt.cpp:285-298
+QDT_API size_t qdt_point_is_used(const qdt_t* ptr, size_t id)
+{
+    const Context* c = ctx(ptr);
+    if (!c) return 0;
+    if (id >= c->npoints() || id >= c->rep.size()) return 0;
+    if (c->tris.empty()) return 0;
+    return c->rep[id] == id ? 1 : 0;
+}
+
+QDT_API void qdt_destroy(qdt_t* ptr) { delete ctx(ptr); }
+
+// ---------------------------------------------------------------------------
+// qdt_gpu.h
+// ---------------------------------------------------------------------------
+
+QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_timing)
+{
+    Context* c = ctx(ptr);
+    if (!c) return;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return;
+    c->engine->set_count_filter(count_filter_failures != 0);
+    c->engine->set_timing(stage_timing != 0);
+}
+
+QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !info) return 0;
+    *info = qdtg_run_info{};
+    if (!c->engine) return 1;
+    const qdtg::RunInfo& r = c->engine->info();
+    info->n = r.n;
+    info->unique_points = r.unique_points;
+    info->triangles = r.ntri;
+    info->orient_exact = r.orient_exact;
+    info->incircle_exact = r.incircle_exact;
+    info->ms_h2d = r.ms.h2d;
+    info->ms_sort = r.ms.keys_sort;
+    info->ms_unique = r.ms.unique;
+    info->ms_split = r.ms.split;
+    info->ms_build = r.ms.build;
+    info->ms_extract = r.ms.extract;
+    info->ms_d2h = r.ms.d2h;
+    info->ms_total = r.ms.total;
+    info->device_flags = r.device_status;
+    info->kernel_launches = r.launches;
+    return 1;
+}
+
+QDT_API void* qdtg_stream(const qdt_t* ptr)
+{
+    const Context* c = ctx(ptr);
+    return (c && c->engine) ? reinterpret_cast<void*>(c->engine->stream()) : nullptr;
+}
+
+QDT_API qdt_status qdtg_execute_device(qdt_t* ptr, const qdt_vec2d* d_pts, size_t n, void* cuda_stream)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    try
+    {
+        c->reset();
+        if (n > qdtg::kMaxPoints) return QDT_ERR_TOO_MANY_POINTS;
+        if (n > 0 && !d_pts) return QDT_ERR_NULL_ARGUMENT;
+        int st = qdtg::ensure_engine(*c);
+        if (st != QDT_OK) return (qdt_status)st;
+        st = c->engine->run_device(reinterpret_cast<const double*>(d_pts), n,
+            reinterpret_cast<cudaStream_t>(cuda_stream));
+        return (qdt_status)st;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        return st;
+    }
+}
+
+QDT_API size_t qdtg_device_triangles(const qdt_t* ptr, const uint32_t** d_tris)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !c->engine) return 0;
+    if (d_tris) *d_tris = c->engine->device_triangles();
+    return c->engine->last_ntri();
+}
+
+QDT_API size_t qdtg_download_device_triangles(const qdt_t* ptr, uint32_t* out, size_t cap)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !c->engine || !out) return 0;
+    const size_t k = std::min(cap, c->engine->last_ntri());
+    if (k == 0) return 0;
+    if (cudaMemcpy(out, c->engine->device_triangles(), 3 * k * sizeof(uint32_t), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+    {
+        cudaGetLastError();
+        return 0;
+    }
+    return k;
+}
+
+QDT_API size_t qdtg_copy_triangles(const qdt_t* ptr, uint32_t* out, size_t cap)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !out) return 0;
+    const size_t k = std::min(cap, c->ntris());
+    std::copy(c->tris.data(), c->tris.data() + 3 * k, out);
+    return k;
+}
+
+QDT_API size_t qdtg_copy_rep(const qdt_t* ptr, uint32_t* out, size_t cap)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !out) return 0;
+    const size_t k = std::min(cap, c->rep.size());
+    std::copy(c->rep.data(), c->rep.data() + k, out);
+    return k;
+}
+
+QDT_API int qdtg_last_cuda_error(const qdt_t* ptr)
+{
+    const Context* c = ctx(ptr);
+    return c ? c->last_cuda_error : 0;
+}
+
+QDT_API const char* qdtg_version(void) { return "qdt-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

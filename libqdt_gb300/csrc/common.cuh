@@ -1,0 +1,96 @@
+// Shared device-side types of the GB300 batch triangulation engine.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qdtg {
+
+// One quad-edge record (reference builder.hxx:82-86 keeps next[4] + vtx[2] in
+// 24 bytes). Here a record is 32 bytes, aligned, so that one 32-byte sector
+// fetch brings all of it: onext of its four edges, and the origins of its two
+// primal edges. Edge id = 4 * record + rotation, as in the reference.
+struct __align__(16) Rec
+{
+    int nx[4];
+    int org[2];
+    int link;    // free-list link while the record is dead
+    int pad;
+};
+
+// Per-node state handed from a level to its parent level: the two hull edges
+// the reference's build() returns (builder.hxx:303-348), and the node's free
+// list of dead records (head, tail; -1 when empty).
+struct __align__(16) NodeOut
+{
+    int le, re;
+    int fhead, ftail;
+};
+
+// Device status word: bit flags; 0 means fine.
+enum StatusBits : unsigned
+{
+    ST_NOT_FINITE = 1u,      // an input coordinate is NaN or infinite
+    ST_POOL_EMPTY = 2u,      // a node's free list ran dry (cannot happen with a sound 3n bound)
+    ST_GUARD = 4u,           // a loop exceeded its iteration guard (internal error)
+    ST_BAD_INDEX = 8u,       // an index left its node's range (internal error)
+};
+
+// Filter failures: predicate calls that took the exact integer path.
+struct PredCounters
+{
+    unsigned long long orient_exact, incircle_exact;
+};
+
+struct DevStatus
+{
+    unsigned     flags;
+    unsigned     pad;
+    PredCounters pc;
+};
+
+// The Dwyer split tree depends only on the number m of distinct points: the
+// root covers [0, m); a node [lo, hi) of at least 4 points splits at
+// lo + (hi - lo) / 2 (reference builder.hxx:306-308). Depth d, heap-style
+// index k (bit d-1-l of k = the branch taken at depth l).
+// Returns false when the node does not exist (an ancestor is a leaf).
+__host__ __device__ inline bool node_range(int m, int d, long long k, int& lo, int& hi)
+{
+    lo = 0;
+    hi = m;
+    for (int l = 0; l < d; ++l)
+    {
+        if (hi - lo < 4) return false;
+        const int mid = lo + (hi - lo) / 2;
+        if ((k >> (d - 1 - l)) & 1) lo = mid;
+        else hi = mid;
+    }
+    return true;
+}
+
+// The node at depth <= d that contains position i: stops early at a leaf.
+// Returns the depth reached.
+__host__ __device__ inline int node_of(int m, int d, int i, int& lo, int& hi)
+{
+    lo = 0;
+    hi = m;
+    for (int l = 0; l < d; ++l)
+    {
+        if (hi - lo < 4) return l;
+        const int mid = lo + (hi - lo) / 2;
+        if (i < mid) hi = mid;
+        else lo = mid;
+    }
+    return d;
+}
+
+// Kernels launched by the calling host thread (the engine resets it per call
+// and reports it).
+inline int& launch_counter()
+{
+    static thread_local int c = 0;
+    return c;
+}
+
+}  // namespace qdtg

@@ -1,0 +1,52 @@
+// The object behind qdt_t: what the reference keeps in wrapper::Triangulation
+// (wrapper.hxx:17-23 -- triangles, rep, unique_points, input_points), stored
+// as 32-bit indices in page-locked host memory so that the GPU results land
+// there directly, plus the engine and the lazily built mesh used by the
+// incremental insertion and the constraints.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+
+#include "engine.hpp"
+
+namespace qdtg {
+
+constexpr size_t kMaxPoints = 100000000;   // reference wrapper.hxx:15
+
+struct Mesh;
+
+struct Context
+{
+    PinnedVec<double>   points;     // 2 per point: x, y (input order, then insertions)
+    PinnedVec<uint32_t> rep;        // lowest index with the same coordinates
+    PinnedVec<uint32_t> tris;       // 3 per triangle, counter-clockwise
+    size_t              unique_points = 0;
+    Engine*             engine = nullptr;
+    int                 last_cuda_error = 0;
+    Mesh*               mesh = nullptr;    // built on the first insertion or constraint
+
+    size_t npoints() const { return points.size() / 2; }
+    size_t ntris() const { return tris.size() / 3; }
+
+    // The empty state: no points, no triangles, no constraints, no mesh.
+    // Does not allocate and does not throw.
+    void reset() noexcept;
+    // reset() and release host memory (after an allocation failure)
+    void reset_release() noexcept;
+
+    ~Context();
+};
+
+// Runs the batch engine on the context's own points (used by the insertion
+// when it rebuilds). Returns a qdt_status value.
+int rebuild_from_points(Context& c);
+
+// mesh.cu -- incremental insertion and constrained edges on the host.
+// Both may throw std::bad_alloc; they return a qdt_status value otherwise.
+int  mesh_insert_point(Context& c, double x, double y, bool parallel_build);
+int  mesh_insert_constraint(Context& c, size_t v0, size_t v1);
+void mesh_destroy(Mesh* m) noexcept;
+
+}  // namespace qdtg

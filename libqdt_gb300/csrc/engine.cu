@@ -1,0 +1,349 @@
+// Host orchestration of the GB300 batch triangulation engine: device
+// workspace, the stage sequence on the context's stream, and the transfers.
+#include <cstring>
+#include <new>
+#include <thread>
+
+#include "engine.hpp"
+#include "engine_kernels.hpp"
+#include "scan.cuh"
+
+namespace qdtg {
+
+// status codes (qdt.h)
+enum
+{
+    S_OK = 0,
+    S_NOT_FINITE = -4,
+    S_OOM = -10,
+    S_INTERNAL = -11
+};
+
+struct HostSmall
+{
+    DevStatus st;
+    uint32_t  words[8];   // [0] distinct points, [1] triangles
+};
+
+struct DeviceWork
+{
+    void*        block = nullptr;
+    size_t       bytes = 0;
+    size_t       cap = 0;      // capacity in points
+    PrepBuffers  prep;
+    BuildBuffers build;
+    double2*     pts = nullptr;
+    uint32_t*    words = nullptr;   // device u32 words: [0] distinct, [1] triangles
+    HostSmall*   hsmall = nullptr;  // pinned
+};
+
+namespace {
+
+struct Carver
+{
+    char*  base;
+    size_t off = 0;
+    template <class T>
+    T* take(size_t count)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+size_t carve(DeviceWork& w, char* base, size_t N)
+{
+    Carver c{ base };
+    const size_t tiles_words = sort_count_words(N);
+    const int    D = split_levels((int)std::max<size_t>(N, 4));
+    const size_t nodes = (size_t)1 << D;
+    PrepBuffers& p = w.prep;
+    BuildBuffers& b = w.build;
+    w.pts = c.take<double2>(N);
+    p.pts = w.pts;
+    for (int i = 0; i < 2; ++i)
+    {
+        p.kx[i] = c.take<uint64_t>(N);
+        p.ky[i] = c.take<uint64_t>(N);
+        p.val[i] = c.take<uint32_t>(N);
+        p.A[i] = c.take<uint32_t>(N);
+        p.B[i] = c.take<uint32_t>(N);
+        b.node[i] = c.take<NodeOut>(nodes);
+    }
+    p.counts = c.take<uint32_t>(tiles_words);
+    p.offs = c.take<uint32_t>(tiles_words);
+    const size_t sw = std::max(scan_scratch_words(3 * N), scan_scratch_words(tiles_words));
+    p.scratch = c.take<uint32_t>(sw);
+    p.uexcl = c.take<uint32_t>(N);
+    p.head = c.take<uint32_t>(N);
+    p.uid = c.take<uint32_t>(N);
+    p.ucoord = c.take<double2>(N);
+    p.rep = c.take<uint32_t>(N);
+    p.side = c.take<uint8_t>(N);
+    p.V = c.take<double2>(N);
+    p.vid = c.take<uint32_t>(N);
+    p.status = c.take<DevStatus>(1);
+    w.words = c.take<uint32_t>(8);
+    p.status_u32 = w.words;
+    b.recs = c.take<Rec>(3 * N);
+    b.V = p.V;
+    b.vid = p.vid;
+    b.tri_mask = c.take<uint8_t>(3 * N);
+    b.tri_off = c.take<uint32_t>(3 * N);
+    b.scratch = p.scratch;
+    b.tris = c.take<uint32_t>(6 * N + 3);
+    b.tri_count = w.words + 1;
+    b.status = p.status;
+    return c.off + 256;
+}
+
+}  // namespace
+
+Engine* Engine::create(int* cuda_error)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+    {
+        int count = 0;
+        e = cudaGetDeviceCount(&count);
+        if (e == cudaSuccess && count == 0) e = cudaErrorNoDevice;
+    }
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        if (cuda_error) *cuda_error = (int)e;
+        return nullptr;
+    }
+    Engine* g = new (std::nothrow) Engine();
+    if (!g) return nullptr;
+    g->device_ = dev;
+    if (cudaStreamCreateWithFlags(&g->stream_, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        cudaGetLastError();
+        delete g;
+        return nullptr;
+    }
+    for (auto& ev : g->ev_)
+        cudaEventCreate(&ev);
+    g->w_ = new (std::nothrow) DeviceWork();
+    if (!g->w_)
+    {
+        delete g;
+        return nullptr;
+    }
+    if (cudaHostAlloc((void**)&g->w_->hsmall, sizeof(HostSmall), cudaHostAllocPortable) != cudaSuccess)
+    {
+        cudaGetLastError();
+        delete g;
+        return nullptr;
+    }
+    return g;
+}
+
+Engine::~Engine()
+{
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (w_)
+    {
+        if (w_->block) cudaFree(w_->block);
+        if (w_->hsmall) cudaFreeHost(w_->hsmall);
+        delete w_;
+    }
+    for (auto& ev : ev_)
+        if (ev) cudaEventDestroy(ev);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Engine::ensure(size_t n)
+{
+    if (n <= w_->cap && w_->block) return S_OK;
+    size_t N = std::max<size_t>(n, 1024);
+    if (w_->cap) N = std::max(N, w_->cap + w_->cap / 4);
+    if (w_->block)
+    {
+        cudaStreamSynchronize(stream_);
+        cudaFree(w_->block);
+        w_->block = nullptr;
+        w_->cap = 0;
+    }
+    const size_t bytes = carve(*w_, nullptr, N);
+    void*        blk = nullptr;
+    if (cudaMalloc(&blk, bytes) != cudaSuccess)
+    {
+        cudaGetLastError();
+        // retry at the exact size
+        N = std::max<size_t>(n, 1024);
+        const size_t b2 = carve(*w_, nullptr, N);
+        if (cudaMalloc(&blk, b2) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return S_OOM;
+        }
+        w_->bytes = b2;
+    }
+    else
+        w_->bytes = bytes;
+    w_->block = blk;
+    w_->cap = N;
+    carve(*w_, static_cast<char*>(blk), N);
+    return S_OK;
+}
+
+const uint32_t* Engine::device_triangles() const { return w_ ? w_->build.tris : nullptr; }
+const uint32_t* Engine::device_rep() const { return w_ ? w_->prep.rep : nullptr; }
+
+int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep)
+{
+    cudaStream_t s = stream_;
+    PrepBuffers& p = w_->prep;
+    BuildBuffers& b = w_->build;
+    HostSmall*   hs = w_->hsmall;
+    info_ = RunInfo();
+    info_.n = n;
+    launch_counter() = 0;
+    if (timing_) cudaEventRecord(ev_[1], s);
+    cudaMemsetAsync(p.status, 0, sizeof(DevStatus), s);
+    cudaMemsetAsync(w_->words, 0, 8 * sizeof(uint32_t), s);
+    launch_keys(p, n, s);
+    launch_sort_points(p, n, s);
+    if (timing_) cudaEventRecord(ev_[2], s);
+    launch_unique(p, n, s);
+    if (timing_) cudaEventRecord(ev_[3], s);
+    cudaMemcpyAsync(&hs->st, p.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hs->words, w_->words, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return S_INTERNAL;
+    if (hs->st.flags & ST_NOT_FINITE) return S_NOT_FINITE;
+    const size_t m = hs->words[0];
+    info_.unique_points = m;
+    b.count_filter = count_filter_ ? 1 : 0;
+    if (m >= 3)
+    {
+        launch_frames(p, m, s);
+        launch_split(p, (int)m, s);
+        launch_finalize(p, (int)m, s);
+        if (timing_) cudaEventRecord(ev_[4], s);
+        launch_build(b, (int)m, s);
+        if (timing_) cudaEventRecord(ev_[5], s);
+        launch_extract(b, (int)m, s);
+    }
+    else
+    {
+        if (timing_)
+        {
+            cudaEventRecord(ev_[4], s);
+            cudaEventRecord(ev_[5], s);
+        }
+    }
+    if (timing_) cudaEventRecord(ev_[6], s);
+    cudaMemcpyAsync(&hs->st, p.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hs->words, w_->words, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (host_io)
+    {
+        // the triangle count is at most 2 m - 5: copy that bound, not a
+        // round trip for the exact count
+        const size_t bound = m >= 3 ? std::min<size_t>(2 * m, host_tri_cap) : 0;
+        if (bound) cudaMemcpyAsync(host_tris, b.tris, 3 * bound * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (n) cudaMemcpyAsync(host_rep, p.rep, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    }
+    if (timing_) cudaEventRecord(ev_[7], s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return S_INTERNAL;
+    info_.launches = launch_counter();
+    info_.device_status = (int)hs->st.flags;
+    info_.orient_exact = hs->st.pc.orient_exact;
+    info_.incircle_exact = hs->st.pc.incircle_exact;
+    info_.ntri = m >= 3 ? hs->words[1] : 0;
+    if (hs->st.flags & (ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX)) return S_INTERNAL;
+    if (timing_)
+    {
+        auto el = [&](int a, int z) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev_[a], ev_[z]);
+            return ms;
+        };
+        info_.ms.keys_sort = el(1, 2);
+        info_.ms.unique = el(2, 3);
+        info_.ms.split = el(3, 4);
+        info_.ms.build = el(4, 5);
+        info_.ms.extract = el(5, 6);
+        info_.ms.d2h = el(6, 7);
+    }
+    return S_OK;
+}
+
+int Engine::run_host(const double* xy, size_t n, PinnedVec<double>& points, PinnedVec<uint32_t>& tris, size_t* ntri,
+    PinnedVec<uint32_t>& rep, size_t* unique_points)
+{
+    if (cudaSetDevice(device_) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return S_INTERNAL;
+    }
+    int st = ensure(n);
+    if (st != S_OK) return st;
+    // host copies the caller's points into the context (pinned) in chunks; the
+    // upload of a chunk overlaps the copy of the next one
+    points.resize(2 * n);
+    rep.resize(n);
+    tris.resize(6 * n + 3);
+    if (timing_) cudaEventRecord(ev_[0], stream_);
+    const size_t chunk = (size_t)1 << 18;   // points per chunk (4 MiB)
+    for (size_t off = 0; off < n; off += chunk)
+    {
+        const size_t c = std::min(chunk, n - off);
+        std::memcpy(points.data() + 2 * off, xy + 2 * off, c * 2 * sizeof(double));
+        cudaMemcpyAsync(w_->pts + off, points.data() + 2 * off, c * sizeof(double2), cudaMemcpyHostToDevice,
+            stream_);
+    }
+    st = pipeline(n, true, tris.data(), (6 * n + 3) / 3, rep.data());
+    if (st != S_OK) return st;
+    if (timing_)
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+        info_.ms.h2d = ms;
+        cudaEventElapsedTime(&ms, ev_[0], ev_[7]);
+        info_.ms.total = ms;
+    }
+    *ntri = info_.ntri;
+    *unique_points = info_.unique_points;
+    tris.resize(3 * info_.ntri);
+    return S_OK;
+}
+
+int Engine::run_device(const double* d_xy, size_t n, cudaStream_t user_stream)
+{
+    if (cudaSetDevice(device_) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return S_INTERNAL;
+    }
+    int st = ensure(n);
+    if (st != S_OK) return st;
+    if (user_stream)
+    {
+        // order after the caller's work on its stream
+        cudaEventRecord(ev_[8], user_stream);
+        cudaStreamWaitEvent(stream_, ev_[8], 0);
+    }
+    if (timing_) cudaEventRecord(ev_[0], stream_);
+    // read the caller's device array in place when it allows 16-byte loads
+    if (((uintptr_t)d_xy & 15) == 0)
+        w_->prep.pts = reinterpret_cast<const double2*>(d_xy);
+    else if (n)
+        cudaMemcpyAsync(w_->pts, d_xy, n * sizeof(double2), cudaMemcpyDeviceToDevice, stream_);
+    st = pipeline(n, false, nullptr, 0, nullptr);
+    w_->prep.pts = w_->pts;
+    if (st == S_OK && timing_)
+    {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev_[0], ev_[7]);
+        info_.ms.total = ms;
+    }
+    return st;
+}
+
+}  // namespace qdtg

@@ -1,0 +1,126 @@
+// The GB300 batch triangulation engine: owns one CUDA stream and the device
+// workspace of one context, runs the kernel stages, and leaves the result in
+// host buffers of the context.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace qdtg {
+
+// Allocator for host buffers that the GPU copies to and from: page-locked
+// memory (cudaHostAlloc), and default-initialisation so that resize() does not
+// clear memory that a copy overwrites anyway.
+template <class T>
+struct PinnedAllocator
+{
+    using value_type = T;
+    PinnedAllocator() = default;
+    template <class U>
+    PinnedAllocator(const PinnedAllocator<U>&) noexcept
+    {
+    }
+    T* allocate(size_t n)
+    {
+        void* p = nullptr;
+        if (n == 0) n = 1;
+        if (cudaHostAlloc(&p, n * sizeof(T), cudaHostAllocPortable) != cudaSuccess)
+        {
+            cudaGetLastError();
+            throw std::bad_alloc();
+        }
+        return static_cast<T*>(p);
+    }
+    void deallocate(T* p, size_t) noexcept
+    {
+        if (p) cudaFreeHost(p);
+    }
+    template <class U>
+    void construct(U* p) noexcept
+    {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a)
+    {
+        ::new (static_cast<void*>(p)) U(static_cast<A&&>(a)...);
+    }
+    template <class U>
+    bool operator==(const PinnedAllocator<U>&) const noexcept
+    {
+        return true;
+    }
+    template <class U>
+    bool operator!=(const PinnedAllocator<U>&) const noexcept
+    {
+        return false;
+    }
+};
+
+template <class T>
+using PinnedVec = std::vector<T, PinnedAllocator<T>>;
+
+struct StageTimes
+{
+    float h2d = 0, keys_sort = 0, unique = 0, split = 0, build = 0, extract = 0, d2h = 0, total = 0;
+};
+
+struct RunInfo
+{
+    size_t                 n = 0, unique_points = 0, ntri = 0;
+    unsigned long long     orient_exact = 0, incircle_exact = 0;
+    StageTimes             ms;
+    int                    device_status = 0;
+    int                    launches = 0;
+};
+
+struct DeviceWork;
+
+class Engine
+{
+public:
+    // nullptr when no usable CUDA device is present
+    static Engine* create(int* cuda_error);
+    ~Engine();
+
+    // Triangulates n host points (already validated for count and NULL).
+    // Copies them into `points` (the context's copy), uploads them, runs the
+    // stages and downloads triangles and representatives.
+    // Returns a qdt_status value (QDT_OK, QDT_ERR_NOT_FINITE,
+    // QDT_ERR_OUT_OF_MEMORY, QDT_ERR_INTERNAL).
+    int run_host(const double* xy, size_t n, PinnedVec<double>& points, PinnedVec<uint32_t>& tris,
+        size_t* ntri, PinnedVec<uint32_t>& rep, size_t* unique_points);
+
+    // Triangulates n points already resident on the device. Triangles stay on
+    // the device (device_triangles()). Returns a qdt_status value.
+    int run_device(const double* d_xy, size_t n, cudaStream_t user_stream);
+
+    const uint32_t* device_triangles() const;
+    const uint32_t* device_rep() const;
+    size_t          last_ntri() const { return info_.ntri; }
+    size_t          last_unique() const { return info_.unique_points; }
+    const RunInfo&  info() const { return info_; }
+    cudaStream_t    stream() const { return stream_; }
+    void            set_count_filter(bool on) { count_filter_ = on; }
+    void            set_timing(bool on) { timing_ = on; }
+
+private:
+    Engine() = default;
+    int  ensure(size_t n);
+    int  pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep);
+
+    int             device_ = 0;
+    cudaStream_t    stream_ = nullptr;
+    DeviceWork*     w_ = nullptr;
+    RunInfo         info_;
+    bool            count_filter_ = false;
+    bool            timing_ = false;
+    cudaEvent_t     ev_[10] = {};
+};
+
+}  // namespace qdtg

@@ -1,0 +1,68 @@
+// Host-side launchers of the engine's kernel stages (one translation unit per
+// stage group, compiled in parallel).
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace qdtg {
+
+struct PrepBuffers
+{
+    const double2* pts = nullptr;       // n input points (device)
+    uint64_t*      kx[2] = { nullptr, nullptr };
+    uint64_t*      ky[2] = { nullptr, nullptr };
+    uint32_t*      val[2] = { nullptr, nullptr };
+    int            sorted = 0;          // which ping-pong half holds sort 1's result
+    uint32_t*      counts = nullptr;    // radix digit counts, 256 per tile
+    uint32_t*      offs = nullptr;
+    uint32_t*      scratch = nullptr;   // scan scratch
+    uint32_t*      uexcl = nullptr;     // n: exclusive scans (unique numbering, split ranks)
+    uint32_t*      head = nullptr;      // m: sorted position of each distinct point's first copy
+    uint32_t*      uid = nullptr;       // m: input index of each distinct point
+    double2*       ucoord = nullptr;    // m: coordinates of each distinct point, (x, y) order
+    uint32_t*      rep = nullptr;       // n
+    uint32_t*      A[2] = { nullptr, nullptr };
+    uint32_t*      B[2] = { nullptr, nullptr };
+    int            acur = 0, bcur = 0;
+    uint8_t*       side = nullptr;      // m
+    double2*       V = nullptr;         // m, leaf order
+    uint32_t*      vid = nullptr;       // m
+    DevStatus*     status = nullptr;
+    uint32_t*      status_u32 = nullptr;   // [0] = number of distinct points
+};
+
+struct BuildBuffers
+{
+    Rec*           recs = nullptr;      // 3 m records
+    const double2* V = nullptr;
+    const uint32_t* vid = nullptr;
+    NodeOut*       node[2] = { nullptr, nullptr };   // ping-pong per level, 2^D entries
+    uint8_t*       tri_mask = nullptr;  // 3 m
+    uint32_t*      tri_off = nullptr;   // 3 m
+    uint32_t*      scratch = nullptr;
+    uint32_t*      tris = nullptr;      // 3 * (2 m) output indices
+    uint32_t*      tri_count = nullptr; // device word
+    DevStatus*     status = nullptr;
+    int            count_filter = 0;    // count filter failures in status
+};
+
+size_t sort_count_words(size_t n);
+int    split_levels(int m);
+
+void launch_keys(const PrepBuffers& b, size_t n, cudaStream_t s);
+void launch_sort_points(PrepBuffers& b, size_t n, cudaStream_t s);
+void launch_unique(const PrepBuffers& b, size_t n, cudaStream_t s);
+void launch_frames(PrepBuffers& b, size_t m, cudaStream_t s);
+void launch_split(PrepBuffers& b, int m, cudaStream_t s);
+void launch_finalize(const PrepBuffers& b, int m, cudaStream_t s);
+
+// builds every level from the deepest to the root
+void launch_build(const BuildBuffers& b, int m, cudaStream_t s);
+void launch_extract(const BuildBuffers& b, int m, cudaStream_t s);
+
+}  // namespace qdtg

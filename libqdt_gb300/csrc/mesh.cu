@@ -1,0 +1,738 @@
+// Incremental point insertion and constrained edges on the handle returned by
+// the batch path (host code; not on the GPU hot path).
+//
+// The batch engine leaves triangles, representatives and points in the
+// context. The first insertion or constraint builds a half-edge mesh from
+// them (reference GuibasStolfiDwyer_Wrapper.cpp:99-202); afterwards the mesh
+// and the context's triangle list are kept in step. The algorithms are the
+// published ones the reference uses, written here from their definitions:
+//
+// * insertion (Wrapper.cpp:531-876): locate the point by a visibility walk
+//   with a scan as fallback; split the triangle it lies in (or the two
+//   triangles of the edge it lies on, or join it to the visible hull edges
+//   when it lies outside); restore the Delaunay property with Lawson flips
+//   that never flip a constrained edge;
+// * constraints (Wrapper.cpp:878-1285): trace the segment through the mesh,
+//   reject it when it crosses a constrained edge or passes through a vertex,
+//   flip the crossed edges away (Sloan 1993), mark the new edge constrained,
+//   and re-legalise with Lawson flips.
+//
+// All geometric decisions use the exact predicates of predicates.cuh.
+#include <algorithm>
+#include <deque>
+#include <unordered_map>
+#include <vector>
+
+#include "context.hpp"
+#include "predicates.cuh"
+#include "qdt.h"
+
+namespace qdtg {
+
+struct MV
+{
+    double   x, y;
+    uint32_t orig;
+    int      he;   // an outgoing half-edge
+};
+
+struct HE
+{
+    int  org;
+    int  twin;
+    int  next;
+    int  tri;
+    bool cons;
+};
+
+struct Mesh
+{
+    std::vector<MV>  v;
+    std::vector<HE>  h;
+    std::vector<int> free_h;
+    std::vector<int> o2l;    // point index -> mesh vertex, -1 when none
+    std::vector<int> t2h;    // triangle -> one of its half-edges
+    int              last = 0;
+};
+
+void mesh_destroy(Mesh* m) noexcept { delete m; }
+
+namespace {
+
+inline int orient(const Mesh& M, int a, int b, double px, double py)
+{
+    const MV &A = M.v[a], &B = M.v[b];
+    return orient2d_sign(A.x, A.y, B.x, B.y, px, py);
+}
+inline int orient3(const Mesh& M, int a, int b, int c) { return orient(M, a, b, M.v[c].x, M.v[c].y); }
+inline int incircle4(const Mesh& M, int a, int b, int c, int d)
+{
+    const MV &A = M.v[a], &B = M.v[b], &C = M.v[c], &D = M.v[d];
+    return incircle_sign(A.x, A.y, B.x, B.y, C.x, C.y, D.x, D.y);
+}
+
+// Builds the half-edge mesh from the context's triangles (Wrapper.cpp:99-202).
+void build_mesh(Context& c, Mesh& M)
+{
+    const size_t T = c.ntris();
+    M.v.clear();
+    M.h.clear();
+    M.free_h.clear();
+    M.t2h.clear();
+    M.last = 0;
+    M.o2l.assign(c.npoints(), -1);
+    M.v.reserve(T / 2 + 8);
+    for (size_t t = 0; t < 3 * T; ++t)
+    {
+        const uint32_t o = c.tris[t];
+        if (M.o2l[o] < 0)
+        {
+            M.o2l[o] = (int)M.v.size();
+            M.v.push_back(MV{ c.points[2 * o], c.points[2 * o + 1], o, -1 });
+        }
+    }
+    M.h.resize(3 * T);
+    M.t2h.resize(T);
+    for (size_t t = 0; t < T; ++t)
+    {
+        const int base = (int)(3 * t);
+        for (int i = 0; i < 3; ++i)
+        {
+            const int a = M.o2l[c.tris[3 * t + i]];
+            M.h[base + i] = HE{ a, -1, base + (i + 1) % 3, (int)t, false };
+            if (M.v[a].he < 0) M.v[a].he = base + i;
+        }
+        M.t2h[t] = base;
+    }
+    // twins: outgoing half-edges grouped by origin (CSR), then for u->w look
+    // among w's outgoing ones for w->u
+    const int        nV = (int)M.v.size();
+    std::vector<int> off(nV + 1, 0), adj(3 * T);
+    for (size_t i = 0; i < 3 * T; ++i) ++off[M.h[i].org + 1];
+    for (int i = 0; i < nV; ++i) off[i + 1] += off[i];
+    {
+        std::vector<int> cur(off.begin(), off.end() - 1);
+        for (size_t i = 0; i < 3 * T; ++i) adj[cur[M.h[i].org]++] = (int)i;
+    }
+    for (size_t i = 0; i < 3 * T; ++i)
+    {
+        if (M.h[i].twin >= 0) continue;
+        const int u = M.h[i].org, w = M.h[M.h[i].next].org;
+        for (int k = off[w]; k < off[w + 1]; ++k)
+        {
+            const int j = adj[k];
+            if (M.h[M.h[j].next].org == u)
+            {
+                M.h[i].twin = j;
+                M.h[j].twin = (int)i;
+                break;
+            }
+        }
+    }
+}
+
+Mesh& ensure_mesh(Context& c)
+{
+    if (!c.mesh)
+    {
+        Mesh* m = new Mesh();
+        try
+        {
+            build_mesh(c, *m);
+        }
+        catch (...)
+        {
+            delete m;
+            throw;
+        }
+        c.mesh = m;
+    }
+    return *c.mesh;
+}
+
+int alloc_he(Mesh& M)
+{
+    if (!M.free_h.empty())
+    {
+        const int k = M.free_h.back();
+        M.free_h.pop_back();
+        return k;
+    }
+    M.h.push_back(HE{ -1, -1, -1, -1, false });
+    return (int)M.h.size() - 1;
+}
+
+void free_he(Mesh& M, int k)
+{
+    M.h[k] = HE{ -1, -1, -1, -1, false };
+    M.free_h.push_back(k);
+}
+
+size_t add_tri(Context& c, Mesh& M, int a, int b, int d, int h0)
+{
+    const size_t t = c.ntris();
+    c.tris.push_back(M.v[a].orig);
+    c.tris.push_back(M.v[b].orig);
+    c.tris.push_back(M.v[d].orig);
+    M.t2h.push_back(h0);
+    return t;
+}
+
+// removes triangle idx by moving the last triangle into its slot
+void remove_tri(Context& c, Mesh& M, size_t idx)
+{
+    const size_t last = c.ntris() - 1;
+    if (idx != last)
+    {
+        for (int i = 0; i < 3; ++i) c.tris[3 * idx + i] = c.tris[3 * last + i];
+        const int moved = M.t2h[last];
+        M.t2h[idx] = moved;
+        int e = moved;
+        do
+        {
+            M.h[e].tri = (int)idx;
+            e = M.h[e].next;
+        } while (e != moved);
+    }
+    c.tris.resize(3 * last);
+    M.t2h.pop_back();
+}
+
+// Visibility walk (Wrapper.cpp:423-486), scan as fallback (:491-521).
+// Returns a half-edge of the triangle containing p (border included), or -1
+// with *hull set to a hull half-edge that p sees.
+int locate(const Mesh& M, size_t ntri, double px, double py, int* hull)
+{
+    *hull = -1;
+    if (M.h.empty() || ntri == 0) return -1;
+    int h = M.last;
+    if (h < 0 || h >= (int)M.h.size() || M.h[h].org < 0)
+    {
+        h = 0;
+        while (h < (int)M.h.size() && M.h[h].org < 0) ++h;
+        if (h >= (int)M.h.size()) return -1;
+    }
+    for (size_t step = 0; step < ntri + 16; ++step)
+    {
+        const int h0 = h, h1 = M.h[h0].next, h2 = M.h[h1].next;
+        if (M.h[h2].next != h0) break;
+        const int o0 = orient(M, M.h[h0].org, M.h[h1].org, px, py);
+        const int o1 = orient(M, M.h[h1].org, M.h[h2].org, px, py);
+        const int o2 = orient(M, M.h[h2].org, M.h[h0].org, px, py);
+        if (o0 >= 0 && o1 >= 0 && o2 >= 0) return h0;
+        const int cross = o0 < 0 ? h0 : (o1 < 0 ? h1 : h2);
+        const int tw = M.h[cross].twin;
+        if (tw < 0)
+        {
+            *hull = cross;
+            return -1;
+        }
+        h = tw;
+    }
+    for (size_t t = 0; t < M.t2h.size(); ++t)
+    {
+        const int h0 = M.t2h[t], h1 = M.h[h0].next, h2 = M.h[h1].next;
+        if (orient(M, M.h[h0].org, M.h[h1].org, px, py) >= 0 && orient(M, M.h[h1].org, M.h[h2].org, px, py) >= 0 &&
+            orient(M, M.h[h2].org, M.h[h0].org, px, py) >= 0)
+            return h0;
+    }
+    for (size_t i = 0; i < M.h.size(); ++i)
+    {
+        const HE& e = M.h[i];
+        if (e.org < 0 || e.twin >= 0) continue;
+        if (orient(M, e.org, M.h[e.next].org, px, py) < 0)
+        {
+            *hull = (int)i;
+            return -1;
+        }
+    }
+    return -1;
+}
+
+// Flips the diagonal h (Wrapper.cpp:942-1009). Before: triangles
+// (a, b, c) with h = a->b and (b, a, d) with twin = b->a. After: (d, c, a)
+// and (c, d, b). Refused unless both new triangles are strictly
+// counter-clockwise, or when h is constrained or on the hull.
+bool flip(Context& c, Mesh& M, int h)
+{
+    const int tw = M.h[h].twin;
+    if (tw < 0 || M.h[h].cons) return false;
+    const int hn = M.h[h].next, hp = M.h[hn].next;
+    const int tn = M.h[tw].next, tp = M.h[tn].next;
+    const int a = M.h[h].org, b = M.h[hn].org, cc = M.h[hp].org, d = M.h[tp].org;
+    if (orient3(M, d, cc, a) <= 0 || orient3(M, cc, d, b) <= 0) return false;
+    // triangle 1: h = d->c, hp = c->a, tn = a->d
+    M.h[h].org = d;
+    M.h[h].next = hp;
+    M.h[hp].next = tn;
+    M.h[tn].next = h;
+    // triangle 2: tw = c->d, tp = d->b, hn = b->c
+    M.h[tw].org = cc;
+    M.h[tw].next = tp;
+    M.h[tp].next = hn;
+    M.h[hn].next = tw;
+    const int t1 = M.h[h].tri, t2 = M.h[tw].tri;
+    M.h[tn].tri = t1;
+    M.h[hn].tri = t2;
+    c.tris[3 * t1 + 0] = M.v[d].orig;
+    c.tris[3 * t1 + 1] = M.v[cc].orig;
+    c.tris[3 * t1 + 2] = M.v[a].orig;
+    c.tris[3 * t2 + 0] = M.v[cc].orig;
+    c.tris[3 * t2 + 1] = M.v[d].orig;
+    c.tris[3 * t2 + 2] = M.v[b].orig;
+    M.t2h[t1] = h;
+    M.t2h[t2] = tw;
+    M.v[a].he = tn;
+    M.v[b].he = hn;
+    M.v[cc].he = hp;
+    M.v[d].he = h;
+    return true;
+}
+
+// Calls f(h) for every half-edge h leaving x until f returns true
+// (Wrapper.cpp:885-923): counter-clockwise from the stored one, then
+// clockwise for hull vertices.
+template <class F>
+void for_each_out(const Mesh& M, int x, F&& f)
+{
+    const int h0 = M.v[x].he;
+    if (h0 < 0) return;
+    const size_t limit = M.h.size();
+    size_t       steps = 0;
+    int          h = h0;
+    for (;;)
+    {
+        if (f(h)) return;
+        if (++steps > limit) return;
+        const int prev = M.h[M.h[h].next].next;
+        const int tw = M.h[prev].twin;
+        if (tw < 0) break;
+        if (tw == h0) return;
+        h = tw;
+    }
+    h = h0;
+    for (;;)
+    {
+        const int tw = M.h[h].twin;
+        if (tw < 0) return;
+        h = M.h[tw].next;
+        if (h == h0) return;
+        if (f(h)) return;
+        if (++steps > limit) return;
+    }
+}
+
+int find_he(const Mesh& M, int u, int w)
+{
+    int found = -1;
+    for_each_out(M, u, [&](int h) {
+        if (M.h[M.h[h].next].org == w)
+        {
+            found = h;
+            return true;
+        }
+        return false;
+    });
+    return found;
+}
+
+void mark_cons(Mesh& M, int h)
+{
+    M.h[h].cons = true;
+    if (M.h[h].twin >= 0) M.h[M.h[h].twin].cons = true;
+}
+
+bool same_direction(const MV& a, const MV& b, const MV& c)
+{
+    auto sg = [](double d) { return d > 0 ? 1 : (d < 0 ? -1 : 0); };
+    const int sx = sg(b.x - a.x) * sg(c.x - a.x);
+    const int sy = sg(b.y - a.y) * sg(c.y - a.y);
+    return sx >= 0 && sy >= 0 && (sx > 0 || sy > 0);
+}
+
+bool segments_cross(const Mesh& M, int a, int b, int c, int d)
+{
+    const int o1 = orient3(M, a, b, c), o2 = orient3(M, a, b, d);
+    const int o3 = orient3(M, c, d, a), o4 = orient3(M, c, d, b);
+    return ((o1 > 0 && o2 < 0) || (o1 < 0 && o2 > 0)) && ((o3 > 0 && o4 < 0) || (o3 < 0 && o4 > 0));
+}
+
+// Lists the edges the open segment u-w crosses, each as the half-edge from
+// the vertex right of u->w to the one on its left (Wrapper.cpp:1050-1106).
+int trace(const Mesh& M, size_t ntri, int u, int w, std::vector<int>& crossed)
+{
+    int  start = -1;
+    bool blocked = false;
+    for_each_out(M, u, [&](int h) {
+        const int hn = M.h[h].next;
+        const int y = M.h[hn].org, z = M.h[M.h[hn].next].org;
+        const int oy = orient3(M, u, y, w), oz = orient3(M, u, z, w);
+        if (oy > 0 && oz < 0)
+        {
+            start = hn;
+            return true;
+        }
+        if ((oy == 0 && same_direction(M.v[u], M.v[y], M.v[w])) ||
+            (oz == 0 && same_direction(M.v[u], M.v[z], M.v[w])))
+        {
+            blocked = true;
+            return true;
+        }
+        return false;
+    });
+    if (blocked) return QDT_ERR_THROUGH_POINT;
+    if (start < 0) return QDT_ERR_INTERNAL;
+    int e = start;
+    for (size_t guard = 0; guard <= ntri; ++guard)
+    {
+        if (M.h[e].cons) return QDT_ERR_CROSSES_CONSTRAINT;
+        crossed.push_back(e);
+        const int tw = M.h[e].twin;
+        if (tw < 0) return QDT_ERR_INTERNAL;
+        const int a = M.h[tw].next, b = M.h[a].next;
+        const int x = M.h[b].org;
+        if (x == w) return QDT_OK;
+        const int o = orient3(M, u, w, x);
+        if (o == 0) return QDT_ERR_THROUGH_POINT;
+        e = o > 0 ? a : b;
+    }
+    return QDT_ERR_INTERNAL;
+}
+
+// Lawson's flips over a stack of half-edges (Wrapper.cpp:1111-1142).
+void legalize(Context& c, Mesh& M, std::vector<int>& stack)
+{
+    while (!stack.empty())
+    {
+        const int h = stack.back();
+        stack.pop_back();
+        if (M.h[h].org < 0) continue;
+        const int tw = M.h[h].twin;
+        if (tw < 0 || M.h[h].cons) continue;
+        const int hn = M.h[h].next, hp = M.h[hn].next;
+        const int tn = M.h[tw].next, tp = M.h[tn].next;
+        const int a = M.h[h].org, b = M.h[hn].org, cc = M.h[hp].org, d = M.h[tp].org;
+        if (incircle4(M, a, b, cc, d) <= 0) continue;
+        if (!flip(c, M, h)) continue;
+        stack.push_back(hp);
+        stack.push_back(hn);
+        stack.push_back(tn);
+        stack.push_back(tp);
+    }
+}
+
+int insert_by_rebuild(Context& c, double x, double y)
+{
+    c.points.push_back(x);
+    c.points.push_back(y);
+    return rebuild_from_points(c);
+}
+
+}  // namespace
+
+int mesh_insert_point(Context& c, double x, double y, bool)
+{
+    if (c.ntris() == 0) return insert_by_rebuild(c, x, y);
+    Mesh& M = ensure_mesh(c);
+    if (M.h.empty()) return insert_by_rebuild(c, x, y);
+
+    int       hull = -1;
+    const int h_start = locate(M, c.ntris(), x, y, &hull);
+    if (h_start < 0 && hull < 0) return insert_by_rebuild(c, x, y);
+    const bool outside = h_start < 0;
+    if (!outside)
+    {
+        // a vertex equal to p is a corner of the triangle that contains it
+        int e = h_start;
+        do
+        {
+            const MV& q = M.v[M.h[e].org];
+            if (q.x == x && q.y == y)
+            {
+                c.points.push_back(x);
+                c.points.push_back(y);
+                c.rep.push_back(q.orig);
+                return QDT_OK;
+            }
+            e = M.h[e].next;
+        } while (e != h_start);
+    }
+    M.last = outside ? hull : h_start;
+
+    const uint32_t id = (uint32_t)c.npoints();
+    c.points.push_back(x);
+    c.points.push_back(y);
+    c.rep.push_back(id);
+    ++c.unique_points;
+    const int nv = (int)M.v.size();
+    M.v.push_back(MV{ x, y, id, -1 });
+    if (M.o2l.size() <= id) M.o2l.resize(id + 1, -1);
+    M.o2l[id] = nv;
+
+    // visible hull edges (outside case)
+    std::vector<int> visible;
+    if (outside)
+    {
+        auto vis = [&](int e) { return orient(M, M.h[e].org, M.h[M.h[e].next].org, x, y) < 0; };
+        auto next_hull = [&](int e) {
+            int k = M.h[e].next;
+            while (M.h[k].twin >= 0) k = M.h[M.h[k].twin].next;
+            return k;
+        };
+        auto prev_hull = [&](int e) {
+            int k = M.h[M.h[e].next].next;
+            while (M.h[k].twin >= 0)
+            {
+                const int t = M.h[k].twin;
+                k = M.h[M.h[t].next].next;
+            }
+            return k;
+        };
+        visible.push_back(hull);
+        for (int e = next_hull(hull); e != hull && vis(e); e = next_hull(e)) visible.push_back(e);
+        for (int e = prev_hull(hull); e != hull && vis(e); e = prev_hull(e)) visible.push_back(e);
+    }
+
+    // the cavity: the triangle that contains p, and the one across the edge p
+    // lies on, if any
+    std::vector<int> cav_he, cav_tri;
+    auto             in_cav = [&](int t) { return std::find(cav_tri.begin(), cav_tri.end(), t) != cav_tri.end(); };
+    int              split_a = -1, split_b = -1;
+    if (!outside)
+    {
+        auto add = [&](int e) {
+            const int t = M.h[e].tri;
+            if (t >= 0 && !in_cav(t))
+            {
+                cav_tri.push_back(t);
+                cav_he.push_back(e);
+            }
+        };
+        add(h_start);
+        int e = h_start;
+        do
+        {
+            const int en = M.h[e].next;
+            if (orient(M, M.h[e].org, M.h[en].org, x, y) == 0)
+            {
+                if (M.h[e].twin >= 0) add(M.h[e].twin);
+                if (M.h[e].cons)
+                {
+                    split_a = M.h[e].org;
+                    split_b = M.h[en].org;
+                }
+            }
+            e = en;
+        } while (e != h_start);
+    }
+
+    struct Bnd
+    {
+        int  a, b, ext;
+        bool cons;
+    };
+    std::vector<Bnd> bnd;
+    for (int h0 : cav_he)
+    {
+        int e = h0;
+        do
+        {
+            const int tw = M.h[e].twin;
+            const int twt = tw >= 0 ? M.h[tw].tri : -1;
+            if (!(twt >= 0 && in_cav(twt)))
+            {
+                const int a = M.h[e].org, b = M.h[M.h[e].next].org;
+                if (tw >= 0 || orient(M, a, b, x, y) > 0) bnd.push_back(Bnd{ a, b, tw, M.h[e].cons });
+            }
+            e = M.h[e].next;
+        } while (e != h0);
+    }
+    for (int e : visible)
+    {
+        const int t = M.h[e].tri;
+        if (t >= 0 && in_cav(t)) continue;
+        const int a = M.h[e].org, b = M.h[M.h[e].next].org;
+        bnd.push_back(Bnd{ b, a, e, M.h[e].cons });
+    }
+
+    std::sort(cav_tri.rbegin(), cav_tri.rend());
+    for (int t : cav_tri) remove_tri(c, M, (size_t)t);
+    for (int h0 : cav_he)
+    {
+        int e = h0;
+        do
+        {
+            const int en = M.h[e].next;
+            free_he(M, e);
+            e = en;
+        } while (e != h0);
+    }
+
+    struct NT
+    {
+        int h0, h1, h2;
+    };
+    std::vector<NT> nts;
+    for (const Bnd& q : bnd)
+    {
+        const int h0 = alloc_he(M), h1 = alloc_he(M), h2 = alloc_he(M);
+        M.h[h0] = HE{ q.a, q.ext, h1, -1, q.cons };
+        M.h[h1] = HE{ q.b, -1, h2, -1, false };
+        M.h[h2] = HE{ nv, -1, h0, -1, false };
+        if (q.ext >= 0)
+        {
+            M.h[q.ext].twin = h0;
+            M.h[q.ext].cons = q.cons;
+        }
+        const int t = (int)add_tri(c, M, q.a, q.b, nv, h0);
+        M.h[h0].tri = M.h[h1].tri = M.h[h2].tri = t;
+        nts.push_back(NT{ h0, h1, h2 });
+    }
+    if (nts.empty())
+    {
+        // cannot happen with exact predicates; start over from the points
+        c.points.resize(c.points.size() - 2);
+        c.rep.pop_back();
+        return insert_by_rebuild(c, x, y);
+    }
+    {
+        std::unordered_map<int, int> by_b, by_a;   // b -> (b->p), a -> (p->a)
+        for (const NT& t : nts)
+        {
+            by_b[M.h[t.h1].org] = t.h1;
+            by_a[M.h[t.h0].org] = t.h2;
+        }
+        for (const auto& kv : by_b)
+        {
+            const auto it = by_a.find(kv.first);
+            if (it != by_a.end())
+            {
+                M.h[kv.second].twin = it->second;
+                M.h[it->second].twin = kv.second;
+            }
+        }
+    }
+    M.v[nv].he = nts[0].h2;
+    M.last = nts[0].h0;
+    for (size_t i = 0; i < nts.size(); ++i)
+    {
+        M.v[bnd[i].a].he = nts[i].h0;
+        M.v[bnd[i].b].he = nts[i].h1;
+    }
+    if (split_a >= 0)
+    {
+        for (size_t i = 0; i < nts.size(); ++i)
+        {
+            if (bnd[i].b == split_a || bnd[i].b == split_b) mark_cons(M, nts[i].h1);
+            if (bnd[i].a == split_a || bnd[i].a == split_b) mark_cons(M, nts[i].h2);
+        }
+    }
+
+    // Lawson flips around p: h0 of every new triangle faces p
+    std::vector<int> pending;
+    for (const NT& t : nts) pending.push_back(t.h0);
+    while (!pending.empty())
+    {
+        const int h = pending.back();
+        pending.pop_back();
+        const int tw = M.h[h].twin;
+        if (tw < 0 || M.h[h].cons) continue;
+        const int hn = M.h[h].next, hp = M.h[hn].next;
+        if (M.h[hp].org != nv) continue;
+        const int tn = M.h[tw].next, tp = M.h[tn].next;
+        const int a = M.h[h].org, b = M.h[hn].org, d = M.h[tp].org;
+        if (incircle4(M, a, b, nv, d) <= 0) continue;
+        if (flip(c, M, h))
+        {
+            pending.push_back(tn);
+            pending.push_back(tp);
+        }
+    }
+    return QDT_OK;
+}
+
+int mesh_insert_constraint(Context& c, size_t v0, size_t v1)
+{
+    if (v0 >= c.rep.size() || v1 >= c.rep.size()) return QDT_ERR_INVALID_INDEX;
+    v0 = c.rep[v0];
+    v1 = c.rep[v1];
+    if (v0 == v1) return QDT_ERR_SAME_POINT;
+    Mesh&     M = ensure_mesh(c);
+    const int u = v0 < M.o2l.size() ? M.o2l[v0] : -1;
+    const int w = v1 < M.o2l.size() ? M.o2l[v1] : -1;
+    if (u < 0 || w < 0) return QDT_ERR_NO_TRIANGLES;
+
+    int e = find_he(M, u, w);
+    if (e < 0) e = find_he(M, w, u);
+    if (e >= 0)
+    {
+        mark_cons(M, e);
+        return QDT_OK;
+    }
+    std::vector<int> crossed;
+    const int        tr = trace(M, c.ntris(), u, w, crossed);
+    if (tr != QDT_OK) return tr;
+
+    std::deque<int>  queue(crossed.begin(), crossed.end());
+    std::vector<int> fresh;
+    size_t           stalled = 0;
+    while (!queue.empty())
+    {
+        const int h = queue.front();
+        queue.pop_front();
+        if (flip(c, M, h))
+        {
+            stalled = 0;
+            const int a = M.h[h].org, b = M.h[M.h[h].next].org;
+            if (segments_cross(M, u, w, a, b)) queue.push_back(h);
+            else fresh.push_back(h);
+        }
+        else
+        {
+            queue.push_back(h);
+            if (++stalled >= queue.size()) break;
+        }
+    }
+    bool ok = false;
+    if (queue.empty())
+    {
+        e = -1;
+        for (int h : fresh)
+        {
+            const int a = M.h[h].org, b = M.h[M.h[h].next].org;
+            if ((a == u && b == w) || (a == w && b == u))
+            {
+                e = h;
+                break;
+            }
+        }
+        if (e < 0) e = find_he(M, u, w);
+        if (e < 0) e = find_he(M, w, u);
+        if (e >= 0)
+        {
+            mark_cons(M, e);
+            ok = true;
+        }
+    }
+    std::vector<int> stack;
+    auto             around = [&](int h) {
+        if (M.h[h].org < 0) return;
+        const int n = M.h[h].next;
+        stack.push_back(h);
+        stack.push_back(n);
+        stack.push_back(M.h[n].next);
+        const int tw = M.h[h].twin;
+        if (tw >= 0)
+        {
+            const int tn = M.h[tw].next;
+            stack.push_back(tn);
+            stack.push_back(M.h[tn].next);
+        }
+    };
+    for (int h : fresh) around(h);
+    for (int h : queue) around(h);
+    legalize(c, M, stack);
+    return ok ? QDT_OK : QDT_ERR_INTERNAL;
+}
+
+}  // namespace qdtg

@@ -1085,3 +1085,23 @@ void qdo_result_free(qdo_result* r)
     r->rep = NULL;
     r->ntri = 0;
 }
+
+/* Batched exact signs for the Delaunay checker: out[i] = sign of the
+   predicate on the points whose indices are idx[3 i .. 3 i + 2] (orient) or
+   idx[4 i .. 4 i + 3] (in-circle). */
+void qdo_orient_batch(const double* xy, const int64_t* idx, size_t k, int8_t* out)
+{
+    qdo_stats st;
+    memset(&st, 0, sizeof st);
+    for (size_t i = 0; i < k; ++i)
+        out[i] = (int8_t)orient_sign(xy + 2 * idx[3 * i], xy + 2 * idx[3 * i + 1], xy + 2 * idx[3 * i + 2], &st);
+}
+
+void qdo_incircle_batch(const double* xy, const int64_t* idx, size_t k, int8_t* out)
+{
+    qdo_stats st;
+    memset(&st, 0, sizeof st);
+    for (size_t i = 0; i < k; ++i)
+        out[i] = (int8_t)incircle_sign(xy + 2 * idx[4 * i], xy + 2 * idx[4 * i + 1], xy + 2 * idx[4 * i + 2],
+            xy + 2 * idx[4 * i + 3], &st);
+}

@@ -61,6 +61,10 @@ int qdo_incircle(const double* a, const double* b, const double* c, const double
 int qdo_orient2d_exact(const double* a, const double* b, const double* c);
 int qdo_incircle_exact(const double* a, const double* b, const double* c, const double* d);
 
+/* Batched exact signs (used by the Delaunay checker). */
+void qdo_orient_batch(const double* xy, const int64_t* idx, size_t k, int8_t* out);
+void qdo_incircle_batch(const double* xy, const int64_t* idx, size_t k, int8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

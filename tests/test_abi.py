@@ -1,0 +1,94 @@
+"""The C-ABI library without a GPU: it builds for sm_103a, loads, exports
+every function that include/*.h declares, and its host logic (input checks,
+NULL handling, status strings, the empty context) behaves like the
+reference shim (libqdt/qdt.cpp). Nothing here launches a kernel.
+"""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import libqdt_gb300 as G
+from libqdt_gb300 import qdt_api as Q
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return G.load()
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        names += re.findall(r"QDT_API\s+[\w\s\*]+?\b(\w+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 14 + len(G.GPU_SYMBOLS)
+    for name in names:
+        assert hasattr(lib, name), name
+    for name in Q.QDT_SYMBOLS:
+        assert name in names
+
+
+def test_status_strings(lib):
+    assert lib.qdt_status_string(0) == b"success"
+    assert lib.qdt_status_string(-1) == b"the context is NULL"
+    assert lib.qdt_status_string(-11) == b"internal error"
+    assert lib.qdt_status_string(5) == b"unknown status"
+    assert lib.qdt_status_string(-12) == b"unknown status"
+
+
+def test_null_context(lib):
+    assert lib.qdt_execute(None, None, 0) == Q.QDT_ERR_NULL_CONTEXT
+    assert lib.qdt_execute_parallel(None, None, 0) == Q.QDT_ERR_NULL_CONTEXT
+    idx = ctypes.c_size_t(777)
+    assert lib.qdt_insert_point(None, Q.Vec2d(1, 2), ctypes.byref(idx)) == Q.QDT_ERR_NULL_CONTEXT
+    assert idx.value == 777
+    assert lib.qdt_insert_point_parallel(None, Q.Vec2d(1, 2), None) == Q.QDT_ERR_NULL_CONTEXT
+    assert lib.qdt_insert_constraint(None, 0, 1) == Q.QDT_ERR_NULL_CONTEXT
+    res = (ctypes.c_int * 2)(5, 5)
+    edges = (Q.Edge * 2)()
+    assert lib.qdt_insert_constraints_batch(None, edges, 2, res) == Q.QDT_ERR_NULL_CONTEXT
+    assert list(res) == [Q.QDT_ERR_NULL_CONTEXT] * 2
+    T = (ctypes.c_size_t * 3)(7, 8, 9)
+    assert lib.qdt_triangles_size(None) == 0
+    assert lib.qdt_get_triangle(None, T, 0) == 0 and list(T) == [7, 8, 9]
+    assert lib.qdt_points_size(None) == 0
+    p = Q.Vec2d(3, 4)
+    assert lib.qdt_get_point(None, ctypes.byref(p), 0) == 0 and (p.x, p.y) == (3, 4)
+    assert lib.qdt_point_is_used(None, 0) == 0
+    lib.qdt_destroy(None)
+
+
+def test_host_side_checks_without_gpu(lib):
+    with G.Triangulation(lib) as t:
+        # order of checks: TOO_MANY, then NULL (qdt.cpp:29-43)
+        assert t.execute_raw(None, 100000001) == Q.QDT_ERR_TOO_MANY_POINTS
+        assert t.execute_raw(None, 5) == Q.QDT_ERR_NULL_ARGUMENT
+        assert t.execute_raw(None, 0) == Q.QDT_OK
+        assert t.points_size() == 0 and t.triangles_size() == 0
+        # rejected points and constraints change nothing
+        assert t.insert_point(float("nan"), 0.0)[0] == Q.QDT_ERR_NOT_FINITE
+        assert t.insert_point(0.0, float("inf"))[0] == Q.QDT_ERR_NOT_FINITE
+        assert t.insert_constraint(0, 1) == Q.QDT_ERR_INVALID_INDEX
+        st, res = t.insert_constraints_batch(np.zeros((0, 2)))
+        assert st == Q.QDT_OK
+        assert lib.qdt_insert_constraints_batch(t.ptr, None, 3, None) == Q.QDT_ERR_NULL_ARGUMENT
+        T = (ctypes.c_size_t * 3)(7, 8, 9)
+        assert lib.qdt_get_triangle(t.ptr, T, 0) == 0 and list(T) == [7, 8, 9]
+        assert lib.qdt_get_triangle(t.ptr, None, 0) == 0
+        assert lib.qdt_get_point(t.ptr, None, 0) == 0
+        assert t.point_is_used(0) == 0
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.qdtg_version()

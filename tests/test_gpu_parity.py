@@ -1,0 +1,212 @@
+"""Parity of the GPU batch path with the reference, through the C ABI.
+
+* small structured and random cases: the canonical triangle set and the
+  used-point flags equal the reference's own outputs (tests/golden);
+* the large workloads (up to 4M points): SHA-256 of the canonical set and of
+  the used flags equal the reference's, and the README's published counts;
+* random sets of many shapes: equal to the CPU oracle, triangles and
+  representatives;
+* the exact Delaunay checker finds zero violations on the stress workloads;
+* errors: NaN/inf input gives QDT_ERR_NOT_FINITE and an empty context.
+Integer/index outputs, so every comparison is bit-exact.
+"""
+import hashlib
+import json
+import os
+import threading
+
+import numpy as np
+import pytest
+
+import libqdt_gb300 as G
+from libqdt_gb300 import qdt_api as Q
+from libqdt_gb300 import workloads as W
+from oracle import delaunay_check as D
+from oracle import oracle as O
+from tests.golden import cases as C
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return G.load()
+
+
+def run(lib, pts, parallel=False):
+    with G.Triangulation(lib) as t:
+        st = t.execute(pts, parallel=parallel)
+        return st, t.triangles_array().astype(np.int64), t.rep_array(), t.points_size()
+
+
+def used_flags(tris, n):
+    u = np.zeros(n, dtype=np.uint8)
+    if tris.shape[0]:
+        u[np.unique(tris.ravel())] = 1
+    return u
+
+
+def test_small_cases_equal_reference(lib):
+    d = np.load(os.path.join(GOLDEN, "small_cases.npz"))
+    names = sorted({k.split("/")[0] for k in d.files})
+    for name in names:
+        pts = d[name + "/pts"]
+        for par in (False, True):
+            st, tris, rep, npts = run(lib, pts, par)
+            assert st == 0, name
+            assert npts == pts.shape[0]
+            assert np.array_equal(O.canonical(tris), d[name + "/tris"]), name
+            assert np.array_equal(used_flags(tris, pts.shape[0]), d[name + "/used"]), name
+            with G.Triangulation(lib) as t:
+                t.execute(pts)
+                flags = np.array([t.point_is_used(i) for i in range(pts.shape[0])], dtype=np.uint8)
+            assert np.array_equal(flags, d[name + "/used"]), name
+
+
+with open(os.path.join(GOLDEN, "digests.json")) as _f:
+    _DIGESTS = json.load(_f)["cases"]
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("spec", _DIGESTS, ids=[s["name"] for s in _DIGESTS])
+def test_large_workloads_equal_reference(lib, spec):
+    pts = C.make_large(spec)
+    st, tris, rep, npts = run(lib, pts)
+    assert st == 0
+    ct = O.canonical(tris).astype(np.int64)
+    assert ct.shape[0] == spec["serial"]["ntri"]
+    if "known_ntri" in spec:
+        assert ct.shape[0] == spec["known_ntri"]
+    assert _digest(ct) == spec["serial"]["tri_digest"]
+    used = (rep == np.arange(npts)).astype(np.uint8) if ct.shape[0] else np.zeros(npts, np.uint8)
+    assert _digest(used) == spec["serial"]["used_digest"]
+
+
+def _random_sets():
+    rng = np.random.default_rng(2024)
+    out = []
+    for i in range(120):
+        n = int(rng.integers(0, 3000)) if i % 3 else int(rng.integers(0, 40))
+        kind = i % 6
+        if kind == 0:
+            R = int(rng.choice([1, 2, 3, 5, 10, 100, 1 << 20]))
+            p = rng.integers(-R, R + 1, size=(n, 2)).astype(np.float64)
+        elif kind == 1:
+            p = rng.random((n, 2))
+        elif kind == 2:
+            p = np.round(rng.random((n, 2)) * 64) / 64
+        elif kind == 3:
+            a = rng.integers(0, 360, size=n) * (np.pi / 180)
+            p = np.stack([np.round(1000 * np.cos(a)), np.round(1000 * np.sin(a))], axis=1)
+        elif kind == 4:
+            p = rng.random((n, 2)) * np.ldexp(1.0, int(rng.integers(-900, 900)))
+        else:
+            x = rng.random(n)
+            p = np.stack([x, 0.5 * x + rng.uniform(-1, 1, size=n) * 2.0 ** -40], axis=1)
+        out.append(p)
+    return out
+
+
+def test_random_sets_equal_oracle(lib):
+    for p in _random_sets():
+        st, tris, rep, _ = run(lib, p)
+        o = O.triangulate(p)
+        assert st == 0
+        assert np.array_equal(O.canonical(tris), O.canonical(o.tris))
+        assert np.array_equal(rep, o.rep)
+
+
+@pytest.mark.parametrize("name", ["gauss_300k", "circle_100k", "line_1m", "lattice_512"])
+def test_exact_checker_zero_violations(lib, name):
+    pts = {"gauss_300k": lambda: W.gaussian_mixture(300000, 64, 5),
+           "circle_100k": lambda: W.unit_circle(100000, 6),
+           "line_1m": lambda: W.noisy_line(1000000, 7),
+           "lattice_512": lambda: W.lattice_with_duplicates(512, 0.01, 8)}[name]()
+    st, tris, rep, _ = run(lib, pts)
+    assert st == 0
+    res = D.check(pts, tris, rep)
+    assert D.ok(res), res
+
+
+def test_not_finite_and_recovery(lib):
+    p = W.uniform(1000, 1)
+    bad = p.copy()
+    bad[517, 0] = np.nan
+    with G.Triangulation(lib) as t:
+        assert t.execute(p) == 0 and t.triangles_size() > 0
+        assert t.execute(bad) == Q.QDT_ERR_NOT_FINITE
+        assert t.points_size() == 0 and t.triangles_size() == 0
+        bad[517, 0] = np.inf
+        assert t.execute(bad, parallel=True) == Q.QDT_ERR_NOT_FINITE
+        assert t.execute(p) == 0
+        assert np.array_equal(O.canonical(t.triangles_array()), O.canonical(O.triangulate(p).tris))
+
+
+def test_input_is_copied(lib):
+    p = np.array([[0.0, 0.0], [4.0, 0.0], [3.0, 1.0], [1.0, 1.0]])
+    keep = p.copy()
+    with G.Triangulation(lib) as t:
+        assert t.execute(p) == 0
+        assert np.array_equal(p, keep)
+        p[:] = -999.0
+        assert t.triangles_size() == 2
+        for i in range(4):
+            ok, xy = t.point(i)
+            assert ok == 1 and xy == tuple(keep[i])
+
+
+def test_reuse_and_sizes(lib):
+    # one context, growing and shrinking inputs
+    with G.Triangulation(lib) as t:
+        for n in (10, 100000, 3, 5000, 250000, 0, 7):
+            p = W.uniform(n, n)
+            assert t.execute(p) == 0
+            assert np.array_equal(O.canonical(t.triangles_array()), O.canonical(O.triangulate(p).tris))
+
+
+def test_concurrent_contexts(lib):
+    inputs = [W.uniform(20000 + 1000 * i, 300 + i) for i in range(8)]
+    expect = [O.canonical(O.triangulate(p).tris) for p in inputs]
+    got = [None] * 8
+
+    def work(i):
+        with G.Triangulation(lib) as t:
+            for _ in range(3):
+                assert t.execute(inputs[i], parallel=(i % 2 == 1)) == 0
+            got[i] = O.canonical(t.triangles_array())
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(8)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    for i in range(8):
+        assert np.array_equal(got[i], expect[i])
+
+
+def test_device_resident_path(lib):
+    torch = pytest.importorskip("torch")
+    p = W.uniform(200000, 77)
+    d = torch.from_numpy(p).cuda().contiguous()
+    torch.cuda.synchronize()
+    with G.Triangulation(lib) as t:
+        assert t.execute_device(d.data_ptr(), p.shape[0]) == 0
+        assert t.triangles_size() == 0   # the host side is left empty
+        host = t.download_device_triangles()
+    assert np.array_equal(O.canonical(host), O.canonical(O.triangulate(p).tris))
+
+
+def test_filter_failure_counts(lib):
+    with G.Triangulation(lib) as t:
+        t.set_options(count_filter_failures=True, stage_timing=True)
+        assert t.execute(W.lattice_with_duplicates(256, 0.01, 3)) == 0
+        info = t.run_info()
+        assert info["orient_exact"] > 0 and info["incircle_exact"] > 0
+        assert info["ms_total"] > 0
+        assert t.execute(W.uniform(100000, 4)) == 0
+        info = t.run_info()
+        assert info["incircle_exact"] == 0
