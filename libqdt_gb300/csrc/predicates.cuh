@@ -62,26 +62,26 @@ QDT_HD __forceinline__ int clz64(uint64_t x)   // x != 0
 #endif
 }
 // separately rounded operations (no contraction into FMA)
-QDT_HD __forceinline__ double dmul(double a, double b)
+QDT_HD __forceinline__ double mul_rn(double a, double b)
 {
 #ifdef __CUDA_ARCH__
-    return dmul(a, b);
+    return __dmul_rn(a, b);
 #else
     return a * b;
 #endif
 }
-QDT_HD __forceinline__ double dadd(double a, double b)
+QDT_HD __forceinline__ double add_rn(double a, double b)
 {
 #ifdef __CUDA_ARCH__
-    return dadd(a, b);
+    return __dadd_rn(a, b);
 #else
     return a + b;
 #endif
 }
-QDT_HD __forceinline__ double dsub(double a, double b)
+QDT_HD __forceinline__ double sub_rn(double a, double b)
 {
 #ifdef __CUDA_ARCH__
-    return dsub(a, b);
+    return __dsub_rn(a, b);
 #else
     return a - b;
 #endif
@@ -416,11 +416,11 @@ static QDT_HD __noinline__ int incircle_exact(const double* v)
 QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double by, double cx, double cy,
     PredCounters* ctr = nullptr)
 {
-    const double detleft = dmul(dsub(ax, cx), dsub(by, cy));
-    const double detright = dmul(dsub(ay, cy), dsub(bx, cx));
-    const double det = dsub(detleft, detright);
-    const double mag = dadd(fabs(detleft), fabs(detright));
-    const double bound = dmul(kErrOrient, mag);
+    const double detleft = mul_rn(sub_rn(ax, cx), sub_rn(by, cy));
+    const double detright = mul_rn(sub_rn(ay, cy), sub_rn(bx, cx));
+    const double det = sub_rn(detleft, detright);
+    const double mag = add_rn(fabs(detleft), fabs(detright));
+    const double bound = mul_rn(kErrOrient, mag);
     if ((det > bound || -det > bound) && mag > kFilterFloor) return det > 0 ? 1 : -1;
 #ifdef __CUDA_ARCH__
     if (ctr) atomicAdd(&ctr->orient_exact, 1ull);
@@ -434,22 +434,22 @@ QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double
 QDT_HD __forceinline__ int incircle_sign(double ax, double ay, double bx, double by, double cx, double cy,
     double dx, double dy, PredCounters* ctr = nullptr)
 {
-    const double adx = dsub(ax, dx), ady = dsub(ay, dy);
-    const double bdx = dsub(bx, dx), bdy = dsub(by, dy);
-    const double cdx = dsub(cx, dx), cdy = dsub(cy, dy);
-    const double bdxcdy = dmul(bdx, cdy), cdxbdy = dmul(cdx, bdy);
-    const double cdxady = dmul(cdx, ady), adxcdy = dmul(adx, cdy);
-    const double adxbdy = dmul(adx, bdy), bdxady = dmul(bdx, ady);
-    const double alift = dadd(dmul(adx, adx), dmul(ady, ady));
-    const double blift = dadd(dmul(bdx, bdx), dmul(bdy, bdy));
-    const double clift = dadd(dmul(cdx, cdx), dmul(cdy, cdy));
-    const double det = dadd(dadd(dmul(alift, dsub(bdxcdy, cdxbdy)),
-                                     dmul(blift, dsub(cdxady, adxcdy))),
-        dmul(clift, dsub(adxbdy, bdxady)));
-    const double perm = dadd(dadd(dmul(dadd(fabs(bdxcdy), fabs(cdxbdy)), alift),
-                                      dmul(dadd(fabs(cdxady), fabs(adxcdy)), blift)),
-        dmul(dadd(fabs(adxbdy), fabs(bdxady)), clift));
-    const double bound = dmul(kErrIncircle, perm);
+    const double adx = sub_rn(ax, dx), ady = sub_rn(ay, dy);
+    const double bdx = sub_rn(bx, dx), bdy = sub_rn(by, dy);
+    const double cdx = sub_rn(cx, dx), cdy = sub_rn(cy, dy);
+    const double bdxcdy = mul_rn(bdx, cdy), cdxbdy = mul_rn(cdx, bdy);
+    const double cdxady = mul_rn(cdx, ady), adxcdy = mul_rn(adx, cdy);
+    const double adxbdy = mul_rn(adx, bdy), bdxady = mul_rn(bdx, ady);
+    const double alift = add_rn(mul_rn(adx, adx), mul_rn(ady, ady));
+    const double blift = add_rn(mul_rn(bdx, bdx), mul_rn(bdy, bdy));
+    const double clift = add_rn(mul_rn(cdx, cdx), mul_rn(cdy, cdy));
+    const double det = add_rn(add_rn(mul_rn(alift, sub_rn(bdxcdy, cdxbdy)),
+                                     mul_rn(blift, sub_rn(cdxady, adxcdy))),
+        mul_rn(clift, sub_rn(adxbdy, bdxady)));
+    const double perm = add_rn(add_rn(mul_rn(add_rn(fabs(bdxcdy), fabs(cdxbdy)), alift),
+                                      mul_rn(add_rn(fabs(cdxady), fabs(adxcdy)), blift)),
+        mul_rn(add_rn(fabs(adxbdy), fabs(bdxady)), clift));
+    const double bound = mul_rn(kErrIncircle, perm);
     if ((det > bound || -det > bound) && perm > kFilterFloor) return det > 0 ? 1 : -1;
 #ifdef __CUDA_ARCH__
     if (ctr) atomicAdd(&ctr->incircle_exact, 1ull);
