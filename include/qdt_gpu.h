@@ -80,6 +80,23 @@ QDT_API void* qdtg_stream(const qdt_t* ptr);
    present. */
 QDT_API int qdtg_last_cuda_error(const qdt_t* ptr);
 
+/* The exact predicates of the engine, on the host: the sign (-1, 0, +1) of
+   orient2d(a, b, c) (> 0: counter-clockwise) and of incircle(a, b, c, d)
+   (> 0: d inside the circle through a, b, c, taken counter-clockwise). Each
+   point is two doubles. Exact for every finite input. */
+QDT_API int qdtg_orient2d(const double* a, const double* b, const double* c);
+QDT_API int qdtg_incircle(const double* a, const double* b, const double* c, const double* d);
+
+/* The same predicates evaluated for count items, on the GPU (on_device != 0;
+   allocates device memory for the call) or on the host: kind 0 =
+   orient2d (6 doubles per item: ax ay bx by cx cy), kind 1 = incircle (8
+   doubles). mode 0 = the full predicate, 1 = only the single-precision
+   pre-filter (0 when it cannot decide), 2 = only the exact integer
+   evaluation. Signs go to out. Returns 0, or a negative code on a CUDA
+   failure or bad arguments. */
+QDT_API int qdtg_eval_predicates(int kind, int mode, int on_device, const double* coords, size_t count,
+    int8_t* out);
+
 /* Library version string. */
 QDT_API const char* qdtg_version(void);
 

@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
 GPU_SYMBOLS = ("qdtg_set_options", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
-               "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_version")
+               "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
+               "qdtg_incircle", "qdtg_eval_predicates", "qdtg_version")
 
 
 class RunInfo(ctypes.Structure):
@@ -84,6 +85,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_stream.restype = ctypes.c_void_p
     lib.qdtg_last_cuda_error.argtypes = [P]
     lib.qdtg_last_cuda_error.restype = ctypes.c_int
+    lib.qdtg_orient2d.argtypes = [P, P, P]
+    lib.qdtg_orient2d.restype = ctypes.c_int
+    lib.qdtg_incircle.argtypes = [P, P, P, P]
+    lib.qdtg_incircle.restype = ctypes.c_int
+    lib.qdtg_eval_predicates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_size_t, P]
+    lib.qdtg_eval_predicates.restype = ctypes.c_int
     lib.qdtg_version.argtypes = []
     lib.qdtg_version.restype = ctypes.c_char_p
     _lib = lib
@@ -144,6 +151,21 @@ class Triangulation(qdt_api.Context):
         if n:
             self.lib.qdtg_download_device_triangles(self.ptr, out.ctypes.data, n)
         return out
+
+
+def eval_predicates(kind: str, coords, mode: str = "full", device: bool = False) -> np.ndarray:
+    """Signs of orient2d (kind "orient", coords (k, 6)) or incircle (kind
+    "incircle", coords (k, 8)); mode "full", "f32" (pre-filter only, 0 when
+    undecided) or "exact"."""
+    lib = load()
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    k = c.shape[0]
+    out = np.zeros(k, dtype=np.int8)
+    rc = lib.qdtg_eval_predicates(0 if kind == "orient" else 1, {"full": 0, "f32": 1, "exact": 2}[mode],
+                                  1 if device else 0, c.ctypes.data, k, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("qdtg_eval_predicates failed: %d" % rc)
+    return out
 
 
 def triangulate(pts) -> np.ndarray:

@@ -8,15 +8,19 @@
 namespace qdtg {
 
 // One quad-edge record (reference builder.hxx:82-86 keeps next[4] + vtx[2] in
-// 24 bytes). Here a record is 32 bytes, aligned, so that one 32-byte sector
-// fetch brings all of it: onext of its four edges, and the origins of its two
-// primal edges. Edge id = 4 * record + rotation, as in the reference.
+// 24 bytes). Here a record is 64 bytes, aligned: onext of its four edges, the
+// origins of its two primal edges, and the coordinates of those two origins.
+// A vertex never moves and an edge's origin is set once, when the edge is
+// made, so the copies stay valid; they spare the merge a dependent load of the
+// vertex array after every record load (the merge is a chain of dependent
+// loads). Edge id = 4 * record + rotation, as in the reference.
 struct __align__(16) Rec
 {
-    int nx[4];
-    int org[2];
-    int link;    // free-list link while the record is dead
-    int pad;
+    int     nx[4];
+    int     org[2];
+    int     link;    // free-list link while the record is dead
+    int     pad;
+    double2 p[2];    // coordinates of org[0], org[1]
 };
 
 // Per-node state handed from a level to its parent level: the two hull edges

@@ -7,14 +7,18 @@
 // that the same split tree gives the same topology, also on cocircular and
 // collinear input. What is GB300-specific is the schedule and the memory:
 //
-// * the tree is built bottom-up, one kernel launch per depth; every node of a
-//   depth is one thread (thousands to millions of independent merges per
-//   launch at the deep levels);
+// * the tree is built bottom-up, one kernel launch per depth. At the deep
+//   depths (hundreds of thousands of small merges) every node is one thread;
+//   at the upper depths (few, long merges) every node is one warp, so that the
+//   merges of a depth never share a warp and their load latencies overlap
+//   across warps and SMs instead of serialising on divergence;
 // * the records live in one pool of exactly 3 m records in HBM. Node [lo, hi)
 //   owns records [3 lo, 3 hi) from its leaves; every node threads its dead
 //   records onto a free list that it passes to its parent, and a merge takes
 //   records from that list before anything else. A planar graph on s vertices
 //   has at most 3 s - 6 edges, so the list never runs dry;
+// * a record carries the coordinates of its two origins, so a record load
+//   gives what the predicates need without a second, dependent load;
 // * every record access is bounds-checked and every loop has an iteration
 //   guard; a violation sets a device status bit and ends the thread, and the
 //   host reports QDT_ERR_INTERNAL. No trap, no hang.
@@ -36,15 +40,19 @@ __device__ __forceinline__ bool less_frame(double2 a, double2 b, int frame)
     return a.y < b.y || (a.y == b.y && a.x > b.x);
 }
 
+__device__ __forceinline__ bool ccw(double2 a, double2 b, double2 c, PredCounters* pc)
+{
+    return orient2d_sign(a.x, a.y, b.x, b.y, c.x, c.y, pc) > 0;
+}
+
 struct Builder
 {
-    Rec*           R;
-    int            nrec;
-    const double2* V;
-    DevStatus*     st;
-    PredCounters*  pc;
-    int            fhead, ftail;
-    bool           bad;
+    Rec*          R;
+    int           nrec;
+    DevStatus*    st;
+    PredCounters* pc;
+    int           fhead, ftail;
+    bool          bad;
 
     __device__ __forceinline__ void fail(unsigned bit)
     {
@@ -53,7 +61,8 @@ struct Builder
     }
     __device__ __forceinline__ int chk(int e)
     {
-        if ((unsigned)(e >> 2) >= (unsigned)nrec || e < 0)
+        // one unsigned compare: negative ids wrap to large values
+        if ((unsigned)e >= 4u * (unsigned)nrec)
         {
             fail(ST_BAD_INDEX);
             return 0;
@@ -67,9 +76,10 @@ struct Builder
         e = chk(e);
         return R[e >> 2].nx[e & 3];
     }
+    // e is always an id this thread has just read through onext(), which
+    // checked it
     __device__ __forceinline__ void set_onext(int e, int v)
     {
-        e = chk(e);
         if (bad) return;   // after a failure, write nothing (other threads own other records)
         R[e >> 2].nx[e & 3] = v;
     }
@@ -78,20 +88,16 @@ struct Builder
         e = chk(e);
         return R[e >> 2].org[(e >> 1) & 1];
     }
-    __device__ __forceinline__ int dest(int e) { return org(sym(e)); }
-    __device__ __forceinline__ int oprev(int e) { return rot(onext(rot(e))); }
-    __device__ __forceinline__ int lnext(int e) { return rot(onext(invrot(e))); }
-    __device__ __forceinline__ int rprev(int e) { return onext(sym(e)); }
-
-    __device__ __forceinline__ double2 P(int v)
+    __device__ __forceinline__ double2 porg(int e)
     {
-        if ((unsigned)v >= (unsigned)(nrec / 3))
-        {
-            fail(ST_BAD_INDEX);
-            v = 0;
-        }
-        return V[v];
+        e = chk(e);
+        return R[e >> 2].p[(e >> 1) & 1];
     }
+    __device__ __forceinline__ int     dest(int e) { return org(sym(e)); }
+    __device__ __forceinline__ double2 pdest(int e) { return porg(sym(e)); }
+    __device__ __forceinline__ int     oprev(int e) { return rot(onext(rot(e))); }
+    __device__ __forceinline__ int     lnext(int e) { return rot(onext(invrot(e))); }
+    __device__ __forceinline__ int     rprev(int e) { return onext(sym(e)); }
 
     // free list of the node (records of the subtree that are not in use)
     __device__ int alloc()
@@ -115,8 +121,9 @@ struct Builder
         fhead = k;
     }
 
-    // reference builder.hxx:131-142, with both origins set at once
-    __device__ int make_edge(int o0, int o1)
+    // reference builder.hxx:131-142, with both origins (and their
+    // coordinates) set at once
+    __device__ int make_edge(int o0, int o1, double2 p0, double2 p1)
     {
         if (bad) return 0;
         const int k = alloc();
@@ -125,14 +132,16 @@ struct Builder
         Rec&      r = R[k];
         *reinterpret_cast<int4*>(&r.nx[0]) = make_int4(e, e + 3, e + 2, e + 1);
         *reinterpret_cast<int4*>(&r.org[0]) = make_int4(o0, o1, -1, 0);
+        r.p[0] = p0;
+        r.p[1] = p1;
         return e;
     }
 
     // reference builder.hxx:144-149
     __device__ void splice(int a, int b)
     {
-        const int alpha = rot(onext(a)), beta = rot(onext(b));
         const int ta = onext(a), tb = onext(b);
+        const int alpha = rot(ta), beta = rot(tb);
         set_onext(a, tb);
         set_onext(b, ta);
         const int tal = onext(alpha), tbe = onext(beta);
@@ -143,7 +152,7 @@ struct Builder
     // reference builder.hxx:151-159
     __device__ int connect(int a, int b)
     {
-        const int e = make_edge(dest(a), org(b));
+        const int e = make_edge(dest(a), org(b), pdest(a), porg(b));
         if (bad) return 0;
         splice(e, lnext(a));
         splice(sym(e), b);
@@ -158,24 +167,16 @@ struct Builder
         release(chk(e) >> 2);
     }
 
-    // reference builder.hxx:168-175
-    __device__ bool ccw(int a, int b, int c)
-    {
-        const double2 pa = P(a), pb = P(b), pc_ = P(c);
-        return orient2d_sign(pa.x, pa.y, pb.x, pb.y, pc_.x, pc_.y, pc) > 0;
-    }
-    __device__ bool right_of(int x, int e) { return ccw(x, dest(e), org(e)); }
-    __device__ bool left_of(int x, int e) { return ccw(x, org(e), dest(e)); }
-    __device__ bool in_circle(int a, int b, int c, int d)
+    // reference builder.hxx:171-175: false when two of the vertices coincide
+    __device__ bool in_circle(int a, double2 pa, int b, double2 pb, int c, double2 pc_, int d, double2 pd)
     {
         if (a == d || b == d || c == d || a == b || a == c || b == c) return false;
-        const double2 pa = P(a), pb = P(b), pc_ = P(c), pd = P(d);
         return incircle_sign(pa.x, pa.y, pb.x, pb.y, pc_.x, pc_.y, pd.x, pd.y, pc) > 0;
     }
 
     // reference builder.hxx:177-201. The leaf's points are V[lo, hi), already
     // in the order of the frame; its records are [3 lo, 3 hi).
-    __device__ void leaf(int lo, int hi, int& le, int& re)
+    __device__ void leaf(int lo, int hi, const double2* __restrict__ V, int& le, int& re)
     {
         const int r0 = 3 * lo, r1 = 3 * hi;
         for (int k = r0; k < r1; ++k)
@@ -185,19 +186,20 @@ struct Builder
         }
         fhead = r0;
         ftail = r1 - 1;
-        const int n = hi - lo, s1 = lo, s2 = lo + 1;
+        const int     n = hi - lo, s1 = lo, s2 = lo + 1;
+        const double2 p1 = V[s1], p2 = V[s2];
         if (n == 2)
         {
-            const int a = make_edge(s1, s2);
+            const int a = make_edge(s1, s2, p1, p2);
             le = a;
             re = sym(a);
             return;
         }
-        const int s3 = lo + 2;
-        const int a = make_edge(s1, s2), b = make_edge(s2, s3);
+        const int     s3 = lo + 2;
+        const double2 p3 = V[s3];
+        const int     a = make_edge(s1, s2, p1, p2), b = make_edge(s2, s3, p2, p3);
         splice(sym(a), b);
-        const double2 p1 = P(s1), p2 = P(s2), p3 = P(s3);
-        const int     o = orient2d_sign(p1.x, p1.y, p2.x, p2.y, p3.x, p3.y, pc);
+        const int o = orient2d_sign(p1.x, p1.y, p2.x, p2.y, p3.x, p3.y, pc);
         if (o > 0)
         {
             connect(b, a);
@@ -228,8 +230,10 @@ struct Builder
                 fail(ST_GUARD);
                 return;
             }
-            if (left_of(org(rdi), ldi)) ldi = lnext(ldi);
-            else if (right_of(org(ldi), rdi)) rdi = rprev(rdi);
+            // leftOf(org(rdi), ldi), then rightOf(org(ldi), rdi)
+            const double2 prdi = porg(rdi), pldi = porg(ldi);
+            if (ccw(prdi, pldi, pdest(ldi), pc)) ldi = lnext(ldi);
+            else if (ccw(pldi, pdest(rdi), prdi, pc)) rdi = rprev(rdi);
             else break;
         }
         int basel = connect(sym(rdi), ldi);
@@ -245,51 +249,66 @@ struct Builder
                 fail(ST_GUARD);
                 return;
             }
-            const int bo = org(basel), bd = dest(basel);
+            const int     bo = org(basel), bd = dest(basel);
+            const double2 pbo = porg(basel), pbd = pdest(basel);
             // left candidate (builder.hxx:205-226)
-            int  lc = onext(sym(basel));
-            bool lv = ccw(dest(lc), bd, bo);
+            int     lc = onext(sym(basel));
+            int     lcd = dest(lc);
+            double2 plcd = pdest(lc);
+            bool    lv = ccw(plcd, pbd, pbo, pc);
             if (lv)
             {
                 bool deleted = false;
                 int  j = 0;
-                while (in_circle(bd, bo, dest(lc), dest(onext(lc))))
+                for (;;)
                 {
+                    const int t = onext(lc);
+                    const int td = dest(t);
+                    const double2 ptd = pdest(t);
+                    if (!in_circle(bd, pbd, bo, pbo, lcd, plcd, td, ptd)) break;
                     if (bad || ++j > lim)
                     {
                         fail(ST_GUARD);
                         return;
                     }
-                    const int t = onext(lc);
                     delete_edge(lc);
                     lc = t;
+                    lcd = td;
+                    plcd = ptd;
                     deleted = true;
                 }
-                if (deleted) lv = ccw(dest(lc), bd, bo);
+                if (deleted) lv = ccw(plcd, pbd, pbo, pc);
             }
             // right candidate (builder.hxx:228-249)
-            int  rc = oprev(basel);
-            bool rv = ccw(dest(rc), bd, bo);
+            int     rc = oprev(basel);
+            int     rcd = dest(rc);
+            double2 prcd = pdest(rc);
+            bool    rv = ccw(prcd, pbd, pbo, pc);
             if (rv)
             {
                 bool deleted = false;
                 int  j = 0;
-                while (in_circle(bd, bo, dest(rc), dest(oprev(rc))))
+                for (;;)
                 {
+                    const int t = oprev(rc);
+                    const int td = dest(t);
+                    const double2 ptd = pdest(t);
+                    if (!in_circle(bd, pbd, bo, pbo, rcd, prcd, td, ptd)) break;
                     if (bad || ++j > lim)
                     {
                         fail(ST_GUARD);
                         return;
                     }
-                    const int t = oprev(rc);
                     delete_edge(rc);
                     rc = t;
+                    rcd = td;
+                    prcd = ptd;
                     deleted = true;
                 }
-                if (deleted) rv = ccw(dest(rc), bd, bo);
+                if (deleted) rv = ccw(prcd, pbd, pbo, pc);
             }
             if (!lv && !rv) break;
-            if (!lv || (rv && in_circle(dest(lc), bd, bo, dest(rc))))
+            if (!lv || (rv && in_circle(lcd, plcd, bd, pbd, bo, pbo, rcd, prcd)))
                 basel = connect(rc, sym(basel));
             else
                 basel = connect(sym(basel), sym(lc));
@@ -311,14 +330,14 @@ struct Builder
             }
             const int     nx = rprev(e);
             const int     pv = sym(oprev(e));
-            const double2 pe = P(org(e));
-            const double2 pn = P(org(nx));
+            const double2 pe = porg(e);
+            const double2 pn = porg(nx);
             if (want_max ? less_frame(pe, pn, frame) : less_frame(pn, pe, frame))
             {
                 e = nx;
                 continue;
             }
-            const double2 pp = P(org(pv));
+            const double2 pp = porg(pv);
             if (want_max ? less_frame(pe, pp, frame) : less_frame(pp, pe, frame))
             {
                 e = pv;
@@ -332,21 +351,25 @@ struct Builder
 constexpr unsigned kFatal = ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX;
 
 // One depth of the tree: leaves of that depth are built, internal nodes merge
-// their children's results (written by the previous launch).
+// their children's results (written by the previous launch). WARP: one node
+// per warp (lane 0 works), else one node per thread.
+template <bool WARP>
 __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
     const NodeOut* __restrict__ child, NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count)
 {
-    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long k = WARP ? (g >> 5) : g;
+    if (WARP && (threadIdx.x & 31)) return;
     if (k >= (1ll << d)) return;
     if (*(volatile unsigned*)&st->flags & kFatal) return;
     int lo, hi;
     if (!node_range(m, d, k, lo, hi)) return;
-    Builder B{ R, nrec, V, st, count ? &st->pc : nullptr, -1, -1, false };
+    Builder B{ R, nrec, st, count ? &st->pc : nullptr, -1, -1, false };
     const int n = hi - lo;
     NodeOut   o;
     if (n <= 3)
     {
-        B.leaf(lo, hi, o.le, o.re);
+        B.leaf(lo, hi, V, o.le, o.re);
     }
     else
     {
@@ -396,6 +419,9 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
     out[k] = o;
 }
 
+// Depths with at most this many nodes run one node per warp.
+constexpr long long kWarpNodes = 1 << 14;
+
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 {
     const int D = split_levels(m);
@@ -403,9 +429,18 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
     for (int d = D; d >= 0; --d)
     {
         const long long nodes = 1ll << d;
-        const unsigned  g = (unsigned)((nodes + 127) / 128);
-        k_build_level<<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d, b.status,
-            b.count_filter);
+        if (nodes <= kWarpNodes)
+        {
+            const unsigned g = (unsigned)((nodes * 32 + 127) / 128);
+            k_build_level<true><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
+                b.status, b.count_filter);
+        }
+        else
+        {
+            const unsigned g = (unsigned)((nodes + 127) / 128);
+            k_build_level<false><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
+                b.status, b.count_filter);
+        }
         ++launch_counter();
     }
 }
@@ -416,8 +451,7 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 // counter-clockwise.
 // ---------------------------------------------------------------------------
 
-__global__ void k_tri_mask(const Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
-    uint8_t* __restrict__ mask, DevStatus* st, int count)
+__global__ void k_tri_mask(const Rec* __restrict__ R, int nrec, uint8_t* __restrict__ mask, DevStatus* st, int count)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nrec) return;
@@ -426,8 +460,8 @@ __global__ void k_tri_mask(const Rec* __restrict__ R, int nrec, const double2* _
         mask[k] = 0;
         return;
     }
-    Builder  B{ const_cast<Rec*>(R), nrec, V, st, count ? &st->pc : nullptr, -1, -1, false };
-    uint8_t  mk = 0;
+    Builder B{ const_cast<Rec*>(R), nrec, st, count ? &st->pc : nullptr, -1, -1, false };
+    uint8_t mk = 0;
     if (R[k].org[0] >= 0)
     {
         for (int r = 0; r < 4; r += 2)
@@ -436,8 +470,7 @@ __global__ void k_tri_mask(const Rec* __restrict__ R, int nrec, const double2* _
             const int f = B.lnext(e), g = B.lnext(f);
             if (B.lnext(g) != e) continue;
             if (e > f || e > g) continue;
-            const double2 a = B.P(B.org(e)), b = B.P(B.org(f)), c = B.P(B.org(g));
-            if (orient2d_sign(a.x, a.y, b.x, b.y, c.x, c.y, B.pc) > 0) mk |= (uint8_t)(1 << (r >> 1));
+            if (ccw(B.porg(e), B.porg(f), B.porg(g), B.pc)) mk |= (uint8_t)(1 << (r >> 1));
         }
     }
     mask[k] = B.bad ? 0 : mk;
@@ -475,9 +508,9 @@ __global__ void k_tri_write(const Rec* __restrict__ R, int nrec, const uint8_t* 
 
 void launch_extract(const BuildBuffers& b, int m, cudaStream_t s)
 {
-    const int nrec = 3 * m;
+    const int      nrec = 3 * m;
     const unsigned g = (unsigned)((nrec + 255) / 256);
-    k_tri_mask<<<g, 256, 0, s>>>(b.recs, nrec, b.V, b.tri_mask, b.status, b.count_filter);
+    k_tri_mask<<<g, 256, 0, s>>>(b.recs, nrec, b.tri_mask, b.status, b.count_filter);
     ++launch_counter();
     scan_exclusive(MaskCount{ b.tri_mask }, (size_t)nrec, b.tri_off, b.scratch, b.tri_count, s);
     k_tri_write<<<g, 256, 0, s>>>(b.recs, nrec, b.tri_mask, b.tri_off, b.vid, b.tris);

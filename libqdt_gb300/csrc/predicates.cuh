@@ -410,12 +410,128 @@ static QDT_HD __noinline__ int incircle_exact(const double* v)
 }
 
 // ---------------------------------------------------------------------------
+// Single-precision pre-filter
+// ---------------------------------------------------------------------------
+//
+// The FP64 pipe of this GPU issues 2 lanes per cycle per SM (FP32: 128), and
+// the merges are chains of dependent predicate evaluations. So every
+// predicate first tries a float evaluation with a rigorous error bound; only
+// when that cannot decide does it run the reference's double filter, and
+// then the exact evaluation. The decision is always the exact sign.
+//
+// Derivation (forward error analysis, u = 2^-24). The coordinate differences
+// X are computed in double (relative error <= 2^-53) and truncated to float
+// by integer operations (relative error < 2^-23), so every float difference
+// is x = X (1 + t) with |t| <= 2u (1 + 2^-29). Each float product of two
+// differences then has relative error <= 5u + O(u^2), a lift (sum of two
+// squares) <= 6u, a cross term |C~ - C| <= 5u P + u |C~| with P the sum of
+// the two products' magnitudes, a term L C <= 12u L P, and the two final
+// additions add <= 2u sum(L P). Hence
+//   orient2d: |D~ - D| <= 5u M + u |D~|,   M = |p| + |q|
+//   incircle: |D~ - D| <= 15u perm,        perm = sum_k L_k P_k
+// (the same permanent as the reference's filter). The filter accepts when
+// |D~| > 8u M (orient2d) or |D~| > 24u perm (incircle). Differences outside
+// [2^-60, 2^60) (orient2d) or [2^-30, 2^30) (incircle), zero excepted, are
+// refused, so no float product overflows and none underflows below the
+// normal range by more than the bounds' margin absorbs.
+
+QDT_HD __forceinline__ float f32_bits(uint32_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float f;
+    std::memcpy(&f, &b, sizeof f);
+    return f;
+#endif
+}
+
+// Truncates a double to float with integer operations; clears ok when |v|
+// is nonzero and outside [2^emin, 2^(emax+1)).
+QDT_HD __forceinline__ float trunc_f32(double v, int emin, int emax, bool& ok)
+{
+    const uint64_t b = dbits(v);
+    const uint64_t mag = b & 0x7FFFFFFFFFFFFFFFull;
+    if (mag == 0) return 0.0f;
+    const int e = (int)(mag >> 52) - 1023;
+    if (e < emin || e > emax) ok = false;
+    const uint32_t fb = ((uint32_t)(b >> 63) << 31) | ((uint32_t)(e + 127) << 23) | (uint32_t)((mag >> 29) & 0x7FFFFF);
+    return f32_bits(fb);
+}
+
+QDT_HD __forceinline__ float fmul_(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+QDT_HD __forceinline__ float fadd_(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+QDT_HD __forceinline__ float fsub_(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
+constexpr float kF32Orient = 8.0f * 5.9604644775390625e-08f;     // 8u
+constexpr float kF32Incircle = 24.0f * 5.9604644775390625e-08f;  // 24u
+
+// +1 / -1 when decided, 0 otherwise. acx..bcy are the double differences.
+QDT_HD __forceinline__ int orient2d_f32(double acx, double acy, double bcx, double bcy)
+{
+    bool        ok = true;
+    const float x1 = trunc_f32(acx, -60, 59, ok), x2 = trunc_f32(acy, -60, 59, ok);
+    const float x3 = trunc_f32(bcx, -60, 59, ok), x4 = trunc_f32(bcy, -60, 59, ok);
+    const float p = fmul_(x1, x4), q = fmul_(x2, x3);
+    const float d = fsub_(p, q);
+    const float mag = fadd_(fabsf(p), fabsf(q));
+    const float bound = fmul_(kF32Orient, mag);
+    if (!ok || !(fabsf(d) > bound)) return 0;
+    return d > 0.0f ? 1 : -1;
+}
+
+QDT_HD __forceinline__ int incircle_f32(double adx_, double ady_, double bdx_, double bdy_, double cdx_, double cdy_)
+{
+    bool        ok = true;
+    const float adx = trunc_f32(adx_, -30, 29, ok), ady = trunc_f32(ady_, -30, 29, ok);
+    const float bdx = trunc_f32(bdx_, -30, 29, ok), bdy = trunc_f32(bdy_, -30, 29, ok);
+    const float cdx = trunc_f32(cdx_, -30, 29, ok), cdy = trunc_f32(cdy_, -30, 29, ok);
+    const float bc = fmul_(bdx, cdy), cb = fmul_(cdx, bdy);
+    const float ca = fmul_(cdx, ady), ac = fmul_(adx, cdy);
+    const float ab = fmul_(adx, bdy), ba = fmul_(bdx, ady);
+    const float al = fadd_(fmul_(adx, adx), fmul_(ady, ady));
+    const float bl = fadd_(fmul_(bdx, bdx), fmul_(bdy, bdy));
+    const float cl = fadd_(fmul_(cdx, cdx), fmul_(cdy, cdy));
+    const float det = fadd_(fadd_(fmul_(al, fsub_(bc, cb)), fmul_(bl, fsub_(ca, ac))), fmul_(cl, fsub_(ab, ba)));
+    const float perm = fadd_(fadd_(fmul_(fadd_(fabsf(bc), fabsf(cb)), al), fmul_(fadd_(fabsf(ca), fabsf(ac)), bl)),
+        fmul_(fadd_(fabsf(ab), fabsf(ba)), cl));
+    const float bound = fmul_(kF32Incircle, perm);
+    if (!ok || !(fabsf(det) > bound)) return 0;
+    return det > 0.0f ? 1 : -1;
+}
+
+// ---------------------------------------------------------------------------
 // Filtered predicates (reference robust.hxx:337-347, :377-396)
 // ---------------------------------------------------------------------------
 
 QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double by, double cx, double cy,
     PredCounters* ctr = nullptr)
 {
+    {
+        const int s = orient2d_f32(sub_rn(ax, cx), sub_rn(ay, cy), sub_rn(bx, cx), sub_rn(by, cy));
+        if (s) return s;
+    }
     const double detleft = mul_rn(sub_rn(ax, cx), sub_rn(by, cy));
     const double detright = mul_rn(sub_rn(ay, cy), sub_rn(bx, cx));
     const double det = sub_rn(detleft, detright);
@@ -437,6 +553,10 @@ QDT_HD __forceinline__ int incircle_sign(double ax, double ay, double bx, double
     const double adx = sub_rn(ax, dx), ady = sub_rn(ay, dy);
     const double bdx = sub_rn(bx, dx), bdy = sub_rn(by, dy);
     const double cdx = sub_rn(cx, dx), cdy = sub_rn(cy, dy);
+    {
+        const int s = incircle_f32(adx, ady, bdx, bdy, cdx, cdy);
+        if (s) return s;
+    }
     const double bdxcdy = mul_rn(bdx, cdy), cdxbdy = mul_rn(cdx, bdy);
     const double cdxady = mul_rn(cdx, ady), adxcdy = mul_rn(adx, cdy);
     const double adxbdy = mul_rn(adx, bdy), bdxady = mul_rn(bdx, ady);
