@@ -7,20 +7,28 @@
 
 namespace qdtg {
 
-// One quad-edge record (reference builder.hxx:82-86 keeps next[4] + vtx[2] in
-// 24 bytes). Here a record is 64 bytes, aligned: onext of its four edges, the
-// origins of its two primal edges, and the coordinates of those two origins.
-// A vertex never moves and an edge's origin is set once, when the edge is
-// made, so the copies stay valid; they spare the merge a dependent load of the
-// vertex array after every record load (the merge is a chain of dependent
-// loads). Edge id = 4 * record + rotation, as in the reference.
+// One undirected edge of the planar map (the reference's quad-edge record,
+// builder.hxx:82-86, holds onext of its four rotations). Here the map is kept
+// as two directed half-edges per record, each linked into the ring of edges
+// around its origin in both directions: next = onext (counter-clockwise),
+// prev = oprev (clockwise). That is the same planar map: every query the
+// builder makes -- onext, oprev, lnext = oprev(sym), rprev = onext(sym), org,
+// dest -- has the same answer, but the dual (face) rings are implicit, so
+// making and deleting an edge are ring insertions and removals of a couple of
+// dependent loads instead of four-way splices over the rotations.
+// Half-edge id = 2 * record + direction; sym(e) = e ^ 1.
+// A record is 64 bytes, aligned, and also carries the coordinates of its two
+// origins: a vertex never moves and an edge's origin is set once, when the
+// edge is made, so the copies stay valid; they spare the merge a dependent
+// load of the vertex array after every record load.
 struct __align__(16) Rec
 {
-    int     nx[4];
-    int     org[2];
-    int     link;    // free-list link while the record is dead
+    int     next[2];   // onext of half-edges 2k, 2k+1
+    int     prev[2];   // oprev of half-edges 2k, 2k+1
+    int     org[2];    // origins; org[0] = -1 marks a dead record
+    int     link;      // free-list link while the record is dead
     int     pad;
-    double2 p[2];    // coordinates of org[0], org[1]
+    double2 p[2];      // coordinates of org[0], org[1]
 };
 
 // Per-node state handed from a level to its parent level: the two hull edges

@@ -1,17 +1,19 @@
 // Stages K3-K6 of the batch triangulation: leaves, level-by-level merges with
 // the hull re-walk, and the extraction of triangles.
 //
-// The quad-edge algebra, the leaf construction, the merge (lower common
-// tangent, then the rising bubble with its two candidate scans) and the hull
-// walk follow the reference builder (builder.hxx:123-301) step for step, so
-// that the same split tree gives the same topology, also on cocircular and
-// collinear input. What is GB300-specific is the schedule and the memory:
+// The leaf construction, the merge (lower common tangent, then the rising
+// bubble with its two candidate scans) and the hull walk follow the reference
+// builder (builder.hxx:177-301) step for step, with the same queries on the
+// same planar map, so that the same split tree gives the same topology, also
+// on cocircular and collinear input. What is GB300-specific:
 //
+// * the map is stored as half-edges linked both ways around their origins
+//   (see Rec): the reference's makeEdge/splice/connect/deleteEdge
+//   (builder.hxx:131-166) become ring insertions and removals;
 // * the tree is built bottom-up, one kernel launch per depth. At the deep
 //   depths (hundreds of thousands of small merges) every node is one thread;
-//   at the upper depths (few, long merges) every node is one warp, so that the
-//   merges of a depth never share a warp and their load latencies overlap
-//   across warps and SMs instead of serialising on divergence;
+//   at the upper depths (few, long merges) every node is one warp, and the
+//   warp evaluates the predicates of a bubble step together (warp_merge);
 // * the records live in one pool of exactly 3 m records in HBM. Node [lo, hi)
 //   owns records [3 lo, 3 hi) from its leaves; every node threads its dead
 //   records onto a free list that it passes to its parent, and a merge takes
@@ -29,9 +31,7 @@
 
 namespace qdtg {
 
-__device__ __forceinline__ int rot(int e) { return (e & ~3) | ((e + 1) & 3); }
-__device__ __forceinline__ int invrot(int e) { return (e & ~3) | ((e + 3) & 3); }
-__device__ __forceinline__ int sym(int e) { return e ^ 2; }
+__device__ __forceinline__ int sym(int e) { return e ^ 1; }
 
 // reference builder.hxx:71-76
 __device__ __forceinline__ bool less_frame(double2 a, double2 b, int frame)
@@ -62,7 +62,7 @@ struct Builder
     __device__ __forceinline__ int chk(int e)
     {
         // one unsigned compare: negative ids wrap to large values
-        if ((unsigned)e >= 4u * (unsigned)nrec)
+        if ((unsigned)e >= 2u * (unsigned)nrec)
         {
             fail(ST_BAD_INDEX);
             return 0;
@@ -70,34 +70,41 @@ struct Builder
         return e;
     }
 
-    // reference builder.hxx:123-129
     __device__ __forceinline__ int onext(int e)
     {
         e = chk(e);
-        return R[e >> 2].nx[e & 3];
+        return R[e >> 1].next[e & 1];
     }
-    // e is always an id this thread has just read through onext(), which
-    // checked it
-    __device__ __forceinline__ void set_onext(int e, int v)
+    __device__ __forceinline__ int oprev(int e)
     {
-        if (bad) return;   // after a failure, write nothing (other threads own other records)
-        R[e >> 2].nx[e & 3] = v;
+        e = chk(e);
+        return R[e >> 1].prev[e & 1];
     }
     __device__ __forceinline__ int org(int e)
     {
         e = chk(e);
-        return R[e >> 2].org[(e >> 1) & 1];
+        return R[e >> 1].org[e & 1];
     }
     __device__ __forceinline__ double2 porg(int e)
     {
         e = chk(e);
-        return R[e >> 2].p[(e >> 1) & 1];
+        return R[e >> 1].p[e & 1];
     }
     __device__ __forceinline__ int     dest(int e) { return org(sym(e)); }
     __device__ __forceinline__ double2 pdest(int e) { return porg(sym(e)); }
-    __device__ __forceinline__ int     oprev(int e) { return rot(onext(rot(e))); }
-    __device__ __forceinline__ int     lnext(int e) { return rot(onext(invrot(e))); }
+    __device__ __forceinline__ int     lnext(int e) { return oprev(sym(e)); }
     __device__ __forceinline__ int     rprev(int e) { return onext(sym(e)); }
+
+    // the ids written here were all read through onext/oprev just before,
+    // which checked them
+    __device__ __forceinline__ void set_next(int e, int v)
+    {
+        if (!bad) R[e >> 1].next[e & 1] = v;
+    }
+    __device__ __forceinline__ void set_prev(int e, int v)
+    {
+        if (!bad) R[e >> 1].prev[e & 1] = v;
+    }
 
     // free list of the node (records of the subtree that are not in use)
     __device__ int alloc()
@@ -121,32 +128,38 @@ struct Builder
         fhead = k;
     }
 
-    // reference builder.hxx:131-142, with both origins (and their
-    // coordinates) set at once
+    // reference builder.hxx:131-142: a new edge, alone in the rings of both
+    // its origins, with both origins (and their coordinates) set at once
     __device__ int make_edge(int o0, int o1, double2 p0, double2 p1)
     {
         if (bad) return 0;
         const int k = alloc();
         if (k < 0) return 0;
-        const int e = 4 * k;
+        const int e = 2 * k;
         Rec&      r = R[k];
-        *reinterpret_cast<int4*>(&r.nx[0]) = make_int4(e, e + 3, e + 2, e + 1);
+        *reinterpret_cast<int4*>(&r.next[0]) = make_int4(e, e + 1, e, e + 1);
         *reinterpret_cast<int4*>(&r.org[0]) = make_int4(o0, o1, -1, 0);
         r.p[0] = p0;
         r.p[1] = p1;
         return e;
     }
 
-    // reference builder.hxx:144-149
-    __device__ void splice(int a, int b)
+    // splice(e, x) of an edge e alone in its ring (builder.hxx:144-149):
+    // e follows x counter-clockwise around their common origin
+    __device__ void insert_after(int x, int e)
     {
-        const int ta = onext(a), tb = onext(b);
-        const int alpha = rot(ta), beta = rot(tb);
-        set_onext(a, tb);
-        set_onext(b, ta);
-        const int tal = onext(alpha), tbe = onext(beta);
-        set_onext(alpha, tbe);
-        set_onext(beta, tal);
+        const int n = onext(x);
+        set_next(e, n);
+        set_prev(e, x);
+        set_prev(n, e);
+        set_next(x, e);
+    }
+    // splice(e, oprev(e)): e leaves the ring around its origin
+    __device__ void remove(int e)
+    {
+        const int p = oprev(e), n = onext(e);
+        set_next(p, n);
+        set_prev(n, p);
     }
 
     // reference builder.hxx:151-159
@@ -154,17 +167,18 @@ struct Builder
     {
         const int e = make_edge(dest(a), org(b), pdest(a), porg(b));
         if (bad) return 0;
-        splice(e, lnext(a));
-        splice(sym(e), b);
+        insert_after(lnext(a), e);
+        insert_after(b, sym(e));
         return e;
     }
 
     // reference builder.hxx:161-166
     __device__ void delete_edge(int e)
     {
-        splice(e, oprev(e));
-        splice(sym(e), oprev(sym(e)));
-        release(chk(e) >> 2);
+        e = chk(e);
+        remove(e);
+        remove(sym(e));
+        release(e >> 1);
     }
 
     // reference builder.hxx:171-175: false when two of the vertices coincide
@@ -180,10 +194,7 @@ struct Builder
     {
         const int r0 = 3 * lo, r1 = 3 * hi;
         for (int k = r0; k < r1; ++k)
-        {
-            *reinterpret_cast<int4*>(&R[k].nx[0]) = make_int4(0, 0, 0, 0);
             *reinterpret_cast<int4*>(&R[k].org[0]) = make_int4(-1, -1, k + 1 < r1 ? k + 1 : -1, 0);
-        }
         fhead = r0;
         ftail = r1 - 1;
         const int     n = hi - lo, s1 = lo, s2 = lo + 1;
@@ -198,7 +209,7 @@ struct Builder
         const int     s3 = lo + 2;
         const double2 p3 = V[s3];
         const int     a = make_edge(s1, s2, p1, p2), b = make_edge(s2, s3, p2, p3);
-        splice(sym(a), b);
+        insert_after(sym(a), b);
         const int o = orient2d_sign(p1.x, p1.y, p2.x, p2.y, p3.x, p3.y, pc);
         if (o > 0)
         {
@@ -218,17 +229,17 @@ struct Builder
         re = sym(b);
     }
 
-    // reference builder.hxx:251-285 (with the scans :205-249 in line)
-    __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
+    // lower common tangent (builder.hxx:253-261)
+    __device__ int tangent(int& ldo, int& ldi, int& rdi, int& rdo, int lim)
     {
         int it = 0;
         for (;;)
         {
-            if (bad) return;
+            if (bad) return 0;
             if (++it > lim)
             {
                 fail(ST_GUARD);
-                return;
+                return 0;
             }
             // leftOf(org(rdi), ldi), then rightOf(org(ldi), rdi)
             const double2 prdi = porg(rdi), pldi = porg(ldi);
@@ -236,11 +247,17 @@ struct Builder
             else if (ccw(pldi, pdest(rdi), prdi, pc)) rdi = rprev(rdi);
             else break;
         }
-        int basel = connect(sym(rdi), ldi);
+        const int basel = connect(sym(rdi), ldi);
         if (org(ldi) == org(ldo)) ldo = sym(basel);
         if (org(rdi) == org(rdo)) rdo = basel;
+        return basel;
+    }
 
-        it = 0;
+    // reference builder.hxx:251-285 (with the scans :205-249 in line)
+    __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
+    {
+        int basel = tangent(ldo, ldi, rdi, rdo, lim);
+        int it = 0;
         for (;;)
         {
             if (bad) return;
@@ -262,8 +279,8 @@ struct Builder
                 int  j = 0;
                 for (;;)
                 {
-                    const int t = onext(lc);
-                    const int td = dest(t);
+                    const int     t = onext(lc);
+                    const int     td = dest(t);
                     const double2 ptd = pdest(t);
                     if (!in_circle(bd, pbd, bo, pbo, lcd, plcd, td, ptd)) break;
                     if (bad || ++j > lim)
@@ -290,8 +307,8 @@ struct Builder
                 int  j = 0;
                 for (;;)
                 {
-                    const int t = oprev(rc);
-                    const int td = dest(t);
+                    const int     t = oprev(rc);
+                    const int     td = dest(t);
                     const double2 ptd = pdest(t);
                     if (!in_circle(bd, pbd, bo, pbo, rcd, prcd, td, ptd)) break;
                     if (bad || ++j > lim)
@@ -348,20 +365,148 @@ struct Builder
     }
 };
 
+// ---------------------------------------------------------------------------
+// Warp-cooperative merge (the upper levels)
+// ---------------------------------------------------------------------------
+//
+// The same merge as Builder::merge, with the predicates of one bubble step
+// evaluated by the lanes of a warp at once. Per step, for each side, lanes
+// 0..kWin-1 (left) and 16..16+kWin-1 (right) take the first kWin candidates
+// of the side's ring (c_0 = onext(sym(basel)), c_i+1 = onext(c_i); r_0 =
+// oprev(basel), r_i+1 = oprev(r_i)) and evaluate validE(c_i) and
+// inCircle(bd, bo, dest(c_i), dest(c_i+1)); lanes 4..11 and 20..27 evaluate
+// the final choice inCircle(dest(c_a), bd, bo, dest(r_b)) for all 16 (a, b).
+// Ballots then give how many candidates each scan deletes (the first failing
+// in-circle test), lv, rv and the choice -- the values the reference's
+// sequential loop (builder.hxx:205-283) computes one after the other. The
+// two scans touch disjoint edges (builder.hxx:203-204), so evaluating them
+// together decides the same. Lane 0 alone edits the map (deletions, then the
+// new base edge), in the reference's order; a scan that deletes all kWin
+// candidates continues in another pass. The FP64 and FP32 pipes execute one
+// warp instruction for all lanes, so a wave of 24 predicates costs about one
+// predicate's latency.
+constexpr int kWin = 4;
+
+__device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int      lane = threadIdx.x & 31;
+    const bool     left = lane < 16;
+    const int      j = lane & 15;
+    const bool     slot = j < kWin;
+    const bool     combo = j >= 4 && j < 12;
+    const int      q = left ? (j - 4) : (j + 4);   // combo index 0..15 = 4 a + b
+    const int      ca = q >> 2, rb = q & 3;
+    int            basel = 0;
+    if (lane == 0) basel = B.tangent(ldo, ldi, rdi, rdo, lim);
+    __syncwarp();
+    basel = __shfl_sync(FULL, basel, 0);
+    bool bad = __shfl_sync(FULL, (int)B.bad, 0) != 0;
+    int  it = 0;
+    while (!bad)
+    {
+        if (++it > lim)
+        {
+            if (lane == 0) B.fail(ST_GUARD);
+            break;
+        }
+        const int     bo = B.org(basel), bd = B.dest(basel);
+        const double2 pbo = B.porg(basel), pbd = B.pdest(basel);
+        bool          cont_l = false, cont_r = false;
+        bool          lv = false, rv = false, choice = false;
+        int           lcE = 0, rcE = 0;
+        for (int pass = 0;; ++pass)
+        {
+            if (pass > lim)
+            {
+                if (lane == 0) B.fail(ST_GUARD);
+                bad = true;
+                break;
+            }
+            // the candidate window of this lane's side
+            int c = left ? B.onext(sym(basel)) : B.oprev(basel);
+            const int steps = slot ? j : 0;
+            for (int s = 0; s < steps; ++s) c = left ? B.onext(c) : B.oprev(c);
+            const int     nx = left ? B.onext(c) : B.oprev(c);
+            const int     cd = B.dest(c), nd = B.dest(nx);
+            const double2 pcd = B.pdest(c), pnd = B.pdest(nx);
+            // destinations for the final-choice lanes
+            const int    src_a = combo ? ca : 0, src_b = combo ? 16 + rb : 16;
+            const int    ad = __shfl_sync(FULL, cd, src_a), bdst = __shfl_sync(FULL, cd, src_b);
+            const double ax = __shfl_sync(FULL, pcd.x, src_a), ay = __shfl_sync(FULL, pcd.y, src_a);
+            const double bx = __shfl_sync(FULL, pcd.x, src_b), by = __shfl_sync(FULL, pcd.y, src_b);
+            bool valid = false, inc = false;
+            if (slot) valid = ccw(pcd, pbd, pbo, B.pc);
+            if (slot) inc = B.in_circle(bd, pbd, bo, pbo, cd, pcd, nd, pnd);
+            else if (combo)
+                inc = B.in_circle(ad, make_double2(ax, ay), bd, pbd, bo, pbo, bdst, make_double2(bx, by));
+            const unsigned vm = __ballot_sync(FULL, valid), im = __ballot_sync(FULL, inc);
+            const unsigned vl = vm & 0xFu, il = im & 0xFu, vr = (vm >> 16) & 0xFu, ir = (im >> 16) & 0xFu;
+            const unsigned zl = ~il & 0xFu, zr = ~ir & 0xFu;
+            const int      dl = (cont_l || (vl & 1u)) ? (zl ? __ffs(zl) - 1 : kWin) : 0;
+            const int      dr = (cont_r || (vr & 1u)) ? (zr ? __ffs(zr) - 1 : kWin) : 0;
+            const int      c0 = __shfl_sync(FULL, c, 0), c1 = __shfl_sync(FULL, c, 1);
+            const int      c2 = __shfl_sync(FULL, c, 2), c3 = __shfl_sync(FULL, c, 3);
+            const int      r0 = __shfl_sync(FULL, c, 16), r1 = __shfl_sync(FULL, c, 17);
+            const int      r2 = __shfl_sync(FULL, c, 18), r3 = __shfl_sync(FULL, c, 19);
+            if (lane == 0)
+            {
+                if (dl > 0) B.delete_edge(c0);
+                if (dl > 1) B.delete_edge(c1);
+                if (dl > 2) B.delete_edge(c2);
+                if (dl > 3) B.delete_edge(c3);
+                if (dr > 0) B.delete_edge(r0);
+                if (dr > 1) B.delete_edge(r1);
+                if (dr > 2) B.delete_edge(r2);
+                if (dr > 3) B.delete_edge(r3);
+            }
+            __syncwarp();
+            bad = __any_sync(FULL, B.bad);
+            if (bad) break;
+            if (dl == kWin || dr == kWin)
+            {
+                // a scan used its whole window: it goes on deleting, without
+                // re-testing validity (builder.hxx:216-222)
+                cont_l = cont_l || dl == kWin;
+                cont_r = cont_r || dr == kWin;
+                continue;
+            }
+            lv = (vl >> dl) & 1u;
+            rv = (vr >> dr) & 1u;
+            lcE = dl == 0 ? c0 : dl == 1 ? c1 : dl == 2 ? c2 : c3;
+            rcE = dr == 0 ? r0 : dr == 1 ? r1 : dr == 2 ? r2 : r3;
+            const int ql = dl * 4 + dr;
+            const int qlane = ql < 8 ? 4 + ql : 20 + (ql - 8);
+            choice = (im >> qlane) & 1u;
+            break;
+        }
+        if (bad || (!lv && !rv)) break;
+        const bool take_r = !lv || (rv && choice);
+        if (lane == 0) basel = take_r ? B.connect(rcE, sym(basel)) : B.connect(sym(basel), sym(lcE));
+        __syncwarp();
+        basel = __shfl_sync(FULL, basel, 0);
+        bad = __any_sync(FULL, B.bad);
+    }
+    out_l = __shfl_sync(FULL, ldo, 0);
+    out_r = __shfl_sync(FULL, rdo, 0);
+}
+
 constexpr unsigned kFatal = ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX;
 
 // One depth of the tree: leaves of that depth are built, internal nodes merge
 // their children's results (written by the previous launch). WARP: one node
-// per warp (lane 0 works), else one node per thread.
+// per warp, else one node per thread.
 template <bool WARP>
 __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
     const NodeOut* __restrict__ child, NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count)
 {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long k = WARP ? (g >> 5) : g;
-    if (WARP && (threadIdx.x & 31)) return;
+    const long long k = WARP ? (g >> 5) : g;   // one node per warp: uniform inside the warp
+    const int       lane = WARP ? (int)(threadIdx.x & 31) : 0;
     if (k >= (1ll << d)) return;
-    if (*(volatile unsigned*)&st->flags & kFatal) return;
+    unsigned flags = *(volatile unsigned*)&st->flags;
+    if (WARP) flags = __shfl_sync(0xffffffffu, flags, 0);   // one decision for the whole warp
+    if (flags & kFatal) return;
     int lo, hi;
     if (!node_range(m, d, k, lo, hi)) return;
     Builder B{ R, nrec, st, count ? &st->pc : nullptr, -1, -1, false };
@@ -369,6 +514,7 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
     NodeOut   o;
     if (n <= 3)
     {
+        if (lane != 0) return;
         B.leaf(lo, hi, V, o.le, o.re);
     }
     else
@@ -378,7 +524,7 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
         if ((L.fhead >= 0 && (L.ftail < 3 * lo || L.ftail >= 3 * hi)) ||
             (Rn.fhead >= 0 && (Rn.ftail < 3 * lo || Rn.ftail >= 3 * hi)))
         {
-            B.fail(ST_BAD_INDEX);
+            if (lane == 0) B.fail(ST_BAD_INDEX);
             return;
         }
         // concatenate the children's free lists
@@ -387,7 +533,7 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
             B.fhead = L.fhead;
             if (Rn.fhead >= 0)
             {
-                R[L.ftail].link = Rn.fhead;
+                if (lane == 0) R[L.ftail].link = Rn.fhead;
                 B.ftail = Rn.ftail;
             }
             else
@@ -400,7 +546,9 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
         }
         const int lim = 8 * n + 64;
         int       rl = 0, rr = 0;
-        B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
+        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
+        else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
+        if (lane != 0) return;
         if (d > 0 && !B.bad)
         {
             // reference builder.hxx:340-346: re-pick the extremes in the
@@ -420,7 +568,7 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
 }
 
 // Depths with at most this many nodes run one node per warp.
-constexpr long long kWarpNodes = 1 << 14;
+constexpr long long kWarpNodes = 1 << 12;
 
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 {
@@ -447,7 +595,7 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 
 // ---------------------------------------------------------------------------
 // Extraction (reference builder.hxx:98-116): a face is emitted once, by the
-// smallest of its three edge ids, when it is a 3-cycle oriented
+// smallest of its three half-edge ids, when it is a 3-cycle (lnext) oriented
 // counter-clockwise.
 // ---------------------------------------------------------------------------
 
@@ -464,13 +612,13 @@ __global__ void k_tri_mask(const Rec* __restrict__ R, int nrec, uint8_t* __restr
     uint8_t mk = 0;
     if (R[k].org[0] >= 0)
     {
-        for (int r = 0; r < 4; r += 2)
+        for (int s = 0; s < 2; ++s)
         {
-            const int e = 4 * k + r;
+            const int e = 2 * k + s;
             const int f = B.lnext(e), g = B.lnext(f);
             if (B.lnext(g) != e) continue;
             if (e > f || e > g) continue;
-            if (ccw(B.porg(e), B.porg(f), B.porg(g), B.pc)) mk |= (uint8_t)(1 << (r >> 1));
+            if (ccw(B.porg(e), B.porg(f), B.porg(g), B.pc)) mk |= (uint8_t)(1 << s);
         }
     }
     mask[k] = B.bad ? 0 : mk;
@@ -490,18 +638,15 @@ __global__ void k_tri_write(const Rec* __restrict__ R, int nrec, const uint8_t* 
     const uint8_t mk = mask[k];
     if (!mk) return;
     uint32_t o = off[k];
-    for (int r = 0; r < 4; r += 2)
+    for (int s = 0; s < 2; ++s)
     {
-        if (!(mk & (1 << (r >> 1)))) continue;
-        const int e = 4 * k + r;
-        const int f = rot(R[invrot(e) >> 2].nx[invrot(e) & 3]);
-        const int g = rot(R[invrot(f) >> 2].nx[invrot(f) & 3]);
-        const int a = R[e >> 2].org[(e >> 1) & 1];
-        const int b = R[f >> 2].org[(f >> 1) & 1];
-        const int c = R[g >> 2].org[(g >> 1) & 1];
-        tris[3 * (size_t)o + 0] = vid[a];
-        tris[3 * (size_t)o + 1] = vid[b];
-        tris[3 * (size_t)o + 2] = vid[c];
+        if (!(mk & (1 << s))) continue;
+        const int e = 2 * k + s;
+        const int f = R[sym(e) >> 1].prev[sym(e) & 1];   // lnext(e) = oprev(sym(e))
+        const int g = R[sym(f) >> 1].prev[sym(f) & 1];
+        tris[3 * (size_t)o + 0] = vid[R[e >> 1].org[e & 1]];
+        tris[3 * (size_t)o + 1] = vid[R[f >> 1].org[f & 1]];
+        tris[3 * (size_t)o + 2] = vid[R[g >> 1].org[g & 1]];
         ++o;
     }
 }
