@@ -62,6 +62,10 @@ struct DevStatus
     PredCounters pc;
 };
 
+// Depths whose seams (cut coordinates) are recorded during the split, and whose
+// seam records are prefetched into L2 before they merge.
+constexpr int kSeamDepth = 10;
+
 // The Dwyer split tree depends only on the number m of distinct points: the
 // root covers [0, m); a node [lo, hi) of at least 4 points splits at
 // lo + (hi - lo) / 2 (reference builder.hxx:306-308). Depth d, heap-style

@@ -82,6 +82,8 @@ size_t carve(DeviceWork& w, char* base, size_t N)
     p.ucoord = c.take<double2>(N);
     p.rep = c.take<uint32_t>(N);
     p.side = c.take<uint8_t>(N);
+    p.seam = c.take<double>((size_t)2 << kSeamDepth);
+    b.seam = p.seam;
     p.V = c.take<double2>(N);
     p.vid = c.take<uint32_t>(N);
     p.status = c.take<DevStatus>(1);

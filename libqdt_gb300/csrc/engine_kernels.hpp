@@ -30,6 +30,7 @@ struct PrepBuffers
     uint32_t*      B[2] = { nullptr, nullptr };
     int            acur = 0, bcur = 0;
     uint8_t*       side = nullptr;      // m
+    double*        seam = nullptr;      // 2^(kSeamDepth+1): cut coordinate per upper node
     double2*       V = nullptr;         // m, leaf order
     uint32_t*      vid = nullptr;       // m
     DevStatus*     status = nullptr;
@@ -48,6 +49,7 @@ struct BuildBuffers
     uint32_t*      tris = nullptr;      // 3 * (2 m) output indices
     uint32_t*      tri_count = nullptr; // device word
     DevStatus*     status = nullptr;
+    const double*  seam = nullptr;      // cut coordinates of the upper nodes (PrepBuffers::seam)
     int            count_filter = 0;    // count filter failures in status
 };
 

@@ -107,6 +107,9 @@ struct Builder
     }
 
     // free list of the node (records of the subtree that are not in use)
+    // The link of the popped record is needed only by the next alloc(), so
+    // nothing waits for that load here; the tail is settled by
+    // settle_tail() when the node is done (an emptied list has no tail).
     __device__ int alloc()
     {
         const int k = fhead;
@@ -116,7 +119,6 @@ struct Builder
             return -1;
         }
         fhead = R[k].link;
-        if (fhead < 0) ftail = -1;
         return k;
     }
     __device__ void release(int k)
@@ -126,6 +128,10 @@ struct Builder
         R[k].link = fhead;
         if (fhead < 0) ftail = k;
         fhead = k;
+    }
+    __device__ void settle_tail()
+    {
+        if (fhead < 0) ftail = -1;
     }
 
     // reference builder.hxx:131-142: a new edge, alone in the rings of both
@@ -369,27 +375,76 @@ struct Builder
 // Warp-cooperative merge (the upper levels)
 // ---------------------------------------------------------------------------
 //
-// The same merge as Builder::merge, with the predicates of one bubble step
-// evaluated by the lanes of a warp at once. Per step, for each side, lanes
-// 0..kWin-1 (left) and 16..16+kWin-1 (right) take the first kWin candidates
-// of the side's ring (c_0 = onext(sym(basel)), c_i+1 = onext(c_i); r_0 =
-// oprev(basel), r_i+1 = oprev(r_i)) and evaluate validE(c_i) and
-// inCircle(bd, bo, dest(c_i), dest(c_i+1)); lanes 4..11 and 20..27 evaluate
-// the final choice inCircle(dest(c_a), bd, bo, dest(r_b)) for all 16 (a, b).
-// Ballots then give how many candidates each scan deletes (the first failing
-// in-circle test), lv, rv and the choice -- the values the reference's
-// sequential loop (builder.hxx:205-283) computes one after the other. The
-// two scans touch disjoint edges (builder.hxx:203-204), so evaluating them
-// together decides the same. Lane 0 alone edits the map (deletions, then the
-// new base edge), in the reference's order; a scan that deletes all kWin
-// candidates continues in another pass. The FP64 and FP32 pipes execute one
-// warp instruction for all lanes, so a wave of 24 predicates costs about one
-// predicate's latency.
+// The same merge as Builder::merge, organised around a window of candidates
+// that the warp loads once per bubble step:
+//
+// * left lanes 0..15 walk the ring of bd counter-clockwise from
+//   c_0 = onext(sym(basel)), right lanes 16..31 the ring of bo clockwise from
+//   r_0 = oprev(basel), loading kWin+1 records (c_0..c_4); every lane of a
+//   side loads the same records, so each load is one broadcast transaction;
+// * lanes 0..3 and 16..19 evaluate validE(c_j) and inCircle(bd, bo,
+//   dest(c_j), dest(c_j+1)); lanes 4..11 and 20..27 evaluate the final choice
+//   inCircle(dest(c_a), bd, bo, dest(r_b)) for all 16 (a, b): one wave of
+//   predicates, one warp instruction stream for all of them;
+// * ballots give what the reference's sequential loop (builder.hxx:205-283)
+//   computes one test after the other: how many candidates each scan
+//   deletes (up to the first failing in-circle test), lv, rv and the choice.
+//   The two scans touch disjoint edges (builder.hxx:203-204), so evaluating
+//   them together decides the same;
+// * the map edits need no further loads: the deleted candidates c_0..c_dl-1
+//   are a run of consecutive edges in bd's ring (one link update), and each
+//   one's far end leaves the ring of its other origin using the prev/next of
+//   its own record, already in the window -- one lane per deleted edge; the
+//   new base edge is inserted between neighbours that the window also holds.
+//   The free list takes the deleted records in the reference's order.
+// A scan that deletes its whole window goes on in another pass, without
+// re-testing validity (builder.hxx:216-222). Record indices are clamped to
+// the pool, so no access leaves it; the loops are bounded by guards.
 constexpr int kWin = 4;
+
+struct Ent
+{
+    int     e;    // half-edge
+    int     nx;   // its successor along the scan (onext for the left side, oprev for the right)
+    int     d;    // dest(e)
+    int     fp;   // oprev(sym(e)): neighbours of the far end in the ring of dest(e)
+    int     fn;   // onext(sym(e))
+    double2 p;    // coordinates of dest(e)
+};
+
+__device__ __forceinline__ Ent load_ent(const Rec* __restrict__ R, int e, int nrec, bool left)
+{
+    const int  k = (int)min((unsigned)(e >> 1), (unsigned)(nrec - 1));
+    const int  s = e & 1;
+    const int4 np = *reinterpret_cast<const int4*>(&R[k].next[0]);   // next0 next1 prev0 prev1
+    const int2 og = *reinterpret_cast<const int2*>(&R[k].org[0]);
+    Ent        x;
+    x.e = e;
+    x.nx = left ? (s ? np.y : np.x) : (s ? np.w : np.z);
+    x.d = s ? og.x : og.y;
+    x.fp = s ? np.z : np.w;
+    x.fn = s ? np.x : np.y;
+    x.p = R[k].p[s ^ 1];
+    return x;
+}
+
+__device__ __forceinline__ Rec& recof(Rec* R, int e, int nrec)
+{
+    return R[min((unsigned)(e >> 1), (unsigned)(nrec - 1))];
+}
+__device__ __forceinline__ void st_next(Rec* R, int e, int v, int nrec) { recof(R, e, nrec).next[e & 1] = v; }
+__device__ __forceinline__ void st_prev(Rec* R, int e, int v, int nrec) { recof(R, e, nrec).prev[e & 1] = v; }
+
+__device__ __forceinline__ double2 shfl_d2(double2 v, int src)
+{
+    return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
 
 __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
 {
     const unsigned FULL = 0xffffffffu;
+    Rec* const     R = B.R;
+    const int      nrec = B.nrec;
     const int      lane = threadIdx.x & 31;
     const bool     left = lane < 16;
     const int      j = lane & 15;
@@ -397,12 +452,29 @@ __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int l
     const bool     combo = j >= 4 && j < 12;
     const int      q = left ? (j - 4) : (j + 4);   // combo index 0..15 = 4 a + b
     const int      ca = q >> 2, rb = q & 3;
-    int            basel = 0;
+    const int      jj = slot ? j : 0;               // window slot this lane keeps
+
+    int basel = 0;
     if (lane == 0) basel = B.tangent(ldo, ldi, rdi, rdo, lim);
     __syncwarp();
     basel = __shfl_sync(FULL, basel, 0);
     bool bad = __shfl_sync(FULL, (int)B.bad, 0) != 0;
-    int  it = 0;
+    // free list: head and the link of the head
+    int fhead = __shfl_sync(FULL, B.fhead, 0), ftail = __shfl_sync(FULL, B.ftail, 0);
+    int flink = (fhead >= 0 && !bad) ? recof(R, 2 * fhead, nrec).link : -1;
+    // the base edge, its endpoints and the starts of both windows
+    int     bo = 0, bd = 0, lstart = 0, rstart = 0;
+    double2 pbo = make_double2(0, 0), pbd = pbo;
+    if (!bad)
+    {
+        bo = B.org(basel);
+        bd = B.dest(basel);
+        pbo = B.porg(basel);
+        pbd = B.pdest(basel);
+        lstart = B.onext(sym(basel));
+        rstart = B.oprev(basel);
+    }
+    int it = 0;
     while (!bad)
     {
         if (++it > lim)
@@ -410,11 +482,9 @@ __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int l
             if (lane == 0) B.fail(ST_GUARD);
             break;
         }
-        const int     bo = B.org(basel), bd = B.dest(basel);
-        const double2 pbo = B.porg(basel), pbd = B.pdest(basel);
-        bool          cont_l = false, cont_r = false;
-        bool          lv = false, rv = false, choice = false;
-        int           lcE = 0, rcE = 0;
+        bool cont_l = false, cont_r = false, lv = false, rv = false, choice = false;
+        int  lcE = 0, lcD = 0, lcFn = 0, rcE = 0, rcD = 0, rcFp = 0;
+        double2 lcP = pbo, rcP = pbo;
         for (int pass = 0;; ++pass)
         {
             if (pass > lim)
@@ -423,69 +493,150 @@ __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int l
                 bad = true;
                 break;
             }
-            // the candidate window of this lane's side
-            int c = left ? B.onext(sym(basel)) : B.oprev(basel);
-            const int steps = slot ? j : 0;
-            for (int s = 0; s < steps; ++s) c = left ? B.onext(c) : B.oprev(c);
-            const int     nx = left ? B.onext(c) : B.oprev(c);
-            const int     cd = B.dest(c), nd = B.dest(nx);
-            const double2 pcd = B.pdest(c), pnd = B.pdest(nx);
-            // destinations for the final-choice lanes
-            const int    src_a = combo ? ca : 0, src_b = combo ? 16 + rb : 16;
-            const int    ad = __shfl_sync(FULL, cd, src_a), bdst = __shfl_sync(FULL, cd, src_b);
-            const double ax = __shfl_sync(FULL, pcd.x, src_a), ay = __shfl_sync(FULL, pcd.y, src_a);
-            const double bx = __shfl_sync(FULL, pcd.x, src_b), by = __shfl_sync(FULL, pcd.y, src_b);
-            bool valid = false, inc = false;
-            if (slot) valid = ccw(pcd, pbd, pbo, B.pc);
-            if (slot) inc = B.in_circle(bd, pbd, bo, pbo, cd, pcd, nd, pnd);
-            else if (combo)
-                inc = B.in_circle(ad, make_double2(ax, ay), bd, pbd, bo, pbo, bdst, make_double2(bx, by));
+            // --- the window: kWin + 1 records along this side's ring
+            Ent cur = load_ent(R, left ? lstart : rstart, nrec, left);
+            Ent mine = cur, succ = cur;
+#pragma unroll
+            for (int i = 1; i <= kWin; ++i)
+            {
+                const Ent nx = load_ent(R, cur.nx, nrec, left);
+                if (i == jj) mine = nx;
+                if (i == jj + 1) succ = nx;
+                cur = nx;
+            }
+            // --- one wave of predicates
+            const int     src_a = combo ? ca : 0, src_b = combo ? 16 + rb : 16;
+            const int     ad = __shfl_sync(FULL, mine.d, src_a), bdst = __shfl_sync(FULL, mine.d, src_b);
+            const double2 pa = shfl_d2(mine.p, src_a), pb = shfl_d2(mine.p, src_b);
+            const bool valid = slot && ccw(mine.p, pbd, pbo, B.pc);
+            // one in-circle call for both roles, so the lanes share one
+            // instruction stream: slot (bd, bo, dest c_j, dest c_j+1),
+            // choice (dest c_a, bd, bo, dest r_b)
+            const int     ia = slot ? bd : ad, ib = slot ? bo : bd, ic = slot ? mine.d : bo, id = slot ? succ.d : bdst;
+            const double2 qa = slot ? pbd : pa, qb = slot ? pbo : pbd, qc = slot ? mine.p : pbo,
+                          qd = slot ? succ.p : pb;
+            const bool inc = (slot || combo) && B.in_circle(ia, qa, ib, qb, ic, qc, id, qd);
             const unsigned vm = __ballot_sync(FULL, valid), im = __ballot_sync(FULL, inc);
             const unsigned vl = vm & 0xFu, il = im & 0xFu, vr = (vm >> 16) & 0xFu, ir = (im >> 16) & 0xFu;
             const unsigned zl = ~il & 0xFu, zr = ~ir & 0xFu;
             const int      dl = (cont_l || (vl & 1u)) ? (zl ? __ffs(zl) - 1 : kWin) : 0;
             const int      dr = (cont_r || (vr & 1u)) ? (zr ? __ffs(zr) - 1 : kWin) : 0;
-            const int      c0 = __shfl_sync(FULL, c, 0), c1 = __shfl_sync(FULL, c, 1);
-            const int      c2 = __shfl_sync(FULL, c, 2), c3 = __shfl_sync(FULL, c, 3);
-            const int      r0 = __shfl_sync(FULL, c, 16), r1 = __shfl_sync(FULL, c, 17);
-            const int      r2 = __shfl_sync(FULL, c, 18), r3 = __shfl_sync(FULL, c, 19);
-            if (lane == 0)
+            // the candidate each scan stops at: slot dl (slot kWin is the
+            // successor of slot kWin - 1)
+            const int  srcL = min(dl, kWin - 1), srcR = 16 + min(dr, kWin - 1);
+            const bool overL = dl == kWin, overR = dr == kWin;
+            const int  stopL = overL ? __shfl_sync(FULL, succ.e, srcL) : __shfl_sync(FULL, mine.e, srcL);
+            const int  stopR = overR ? __shfl_sync(FULL, succ.e, srcR) : __shfl_sync(FULL, mine.e, srcR);
+            // --- deletions: far ends (one lane per deleted edge), the
+            // near-end rings, and the free list in the reference's order
+            const int prevrec = __shfl_up_sync(FULL, mine.e >> 1, 1);
+            const int lastL = dl > 0 ? __shfl_sync(FULL, mine.e >> 1, dl - 1) : -1;
+            const int lastR = dr > 0 ? __shfl_sync(FULL, mine.e >> 1, 16 + dr - 1) : -1;
+            const int firstL = __shfl_sync(FULL, mine.e >> 1, 0), firstR = __shfl_sync(FULL, mine.e >> 1, 16);
+            const bool del = slot && j < (left ? dl : dr);
+            if (del)
             {
-                if (dl > 0) B.delete_edge(c0);
-                if (dl > 1) B.delete_edge(c1);
-                if (dl > 2) B.delete_edge(c2);
-                if (dl > 3) B.delete_edge(c3);
-                if (dr > 0) B.delete_edge(r0);
-                if (dr > 1) B.delete_edge(r1);
-                if (dr > 2) B.delete_edge(r2);
-                if (dr > 3) B.delete_edge(r3);
+                st_next(R, mine.fp, mine.fn, nrec);
+                st_prev(R, mine.fn, mine.fp, nrec);
+                Rec&      r = recof(R, mine.e, nrec);
+                const int below = (j > 0) ? prevrec : (left ? fhead : (dl > 0 ? lastL : fhead));
+                r.org[0] = -1;
+                r.link = below;
             }
-            __syncwarp();
-            bad = __any_sync(FULL, B.bad);
-            if (bad) break;
-            if (dl == kWin || dr == kWin)
+            if (lane == 0 && dl > 0)
             {
-                // a scan used its whole window: it goes on deleting, without
-                // re-testing validity (builder.hxx:216-222)
-                cont_l = cont_l || dl == kWin;
-                cont_r = cont_r || dr == kWin;
+                st_next(R, sym(basel), stopL, nrec);
+                st_prev(R, stopL, sym(basel), nrec);
+            }
+            if (lane == 16 && dr > 0)
+            {
+                st_prev(R, basel, stopR, nrec);
+                st_next(R, stopR, basel, nrec);
+            }
+            if (dl + dr > 0)
+            {
+                const int old = fhead;
+                const int newhead = dr > 0 ? lastR : lastL;
+                if (old < 0) ftail = dl > 0 ? firstL : firstR;
+                flink = dr > 1 ? __shfl_sync(FULL, mine.e >> 1, 16 + dr - 2)
+                               : (dr == 1 ? (dl > 0 ? lastL : old) : (dl > 1 ? __shfl_sync(FULL, mine.e >> 1, dl - 2) : old));
+                fhead = newhead;
+            }
+            lstart = stopL;
+            rstart = stopR;
+            __syncwarp();
+            if (overL || overR)
+            {
+                cont_l = cont_l || overL;
+                cont_r = cont_r || overR;
                 continue;
             }
             lv = (vl >> dl) & 1u;
             rv = (vr >> dr) & 1u;
-            lcE = dl == 0 ? c0 : dl == 1 ? c1 : dl == 2 ? c2 : c3;
-            rcE = dr == 0 ? r0 : dr == 1 ? r1 : dr == 2 ? r2 : r3;
+            lcE = stopL;
+            lcD = __shfl_sync(FULL, mine.d, srcL);
+            lcP = shfl_d2(mine.p, srcL);
+            lcFn = __shfl_sync(FULL, mine.fn, srcL);
+            rcE = stopR;
+            rcD = __shfl_sync(FULL, mine.d, srcR);
+            rcP = shfl_d2(mine.p, srcR);
+            rcFp = __shfl_sync(FULL, mine.fp, srcR);
             const int ql = dl * 4 + dr;
             const int qlane = ql < 8 ? 4 + ql : 20 + (ql - 8);
             choice = (im >> qlane) & 1u;
             break;
         }
         if (bad || (!lv && !rv)) break;
+        // --- the new base edge (builder.hxx:279-282), from window values only
         const bool take_r = !lv || (rv && choice);
-        if (lane == 0) basel = take_r ? B.connect(rcE, sym(basel)) : B.connect(sym(basel), sym(lcE));
+        const int  k = fhead;
+        if (k < 0 || k >= nrec)
+        {
+            if (lane == 0) B.fail(ST_POOL_EMPTY);
+            break;
+        }
+        fhead = flink;
+        const int e = 2 * k;
+        int       o0, o1, x0, n0, x1, n1;   // e after x0 (before n0); sym(e) after x1 (before n1)
+        double2   p0, p1;
+        if (take_r)
+        {
+            // connect(rc, sym(basel)): from dest(rc) to bd
+            o0 = rcD, p0 = rcP, o1 = bd, p1 = pbd;
+            x0 = rcFp, n0 = sym(rcE);
+            x1 = sym(basel), n1 = lstart;
+        }
+        else
+        {
+            // connect(sym(basel), sym(lc)): from bo to dest(lc)
+            o0 = bo, p0 = pbo, o1 = lcD, p1 = lcP;
+            x0 = rstart, n0 = basel;
+            x1 = sym(lcE), n1 = lcFn;
+        }
+        if (lane == 0)
+        {
+            Rec& r = R[k];
+            *reinterpret_cast<int4*>(&r.next[0]) = make_int4(n0, n1, x0, x1);
+            *reinterpret_cast<int4*>(&r.org[0]) = make_int4(o0, o1, -1, 0);
+            r.p[0] = p0;
+            r.p[1] = p1;
+            st_next(R, x0, e, nrec);
+            st_prev(R, n0, e, nrec);
+            st_next(R, x1, e + 1, nrec);
+            st_prev(R, n1, e + 1, nrec);
+        }
+        // the next step's base edge and window starts
+        basel = e;
+        bo = o0, pbo = p0, bd = o1, pbd = p1;
+        lstart = n1;   // onext(sym(e))
+        rstart = x0;   // oprev(e)
+        if (fhead >= 0) flink = recof(R, 2 * fhead, nrec).link;
         __syncwarp();
-        basel = __shfl_sync(FULL, basel, 0);
-        bad = __any_sync(FULL, B.bad);
+    }
+    if (lane == 0)
+    {
+        B.fhead = fhead;
+        B.ftail = ftail;
     }
     out_l = __shfl_sync(FULL, ldo, 0);
     out_r = __shfl_sync(FULL, rdo, 0);
@@ -562,9 +713,49 @@ __global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nr
         o.le = rl;
         o.re = rr;
     }
+    B.settle_tail();
     o.fhead = B.fhead;
     o.ftail = B.ftail;
     out[k] = o;
+}
+
+// Before an upper depth merges, the records near its seams are fetched into
+// L2 with the evict-last policy: the merges are chains of dependent loads,
+// and their records were last touched by far deeper levels, so without this
+// a bubble step waits on several DRAM round trips. A record lies near a seam
+// when one of its origins is closer to the cut line than 3 times the edge's
+// own length -- the edges a merge walks or deletes around the seam, at the
+// local scale of the point set. The scan reads the records with streaming
+// (evict-first) loads so that it does not displace what it prefetches.
+__global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int d, const double* __restrict__ seam)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const int4 org = __ldcs(reinterpret_cast<const int4*>(&R[r].org[0]));
+    if (org.x < 0) return;
+    const double2 p0 = __ldcs(&R[r].p[0]), p1 = __ldcs(&R[r].p[1]);
+    // the node of depth d whose record range holds r
+    const int i = r / 3;
+    int       a = 0, b = m;
+    long long k = 0;
+    for (int l = 0; l < d; ++l)
+    {
+        if (b - a < 4) return;
+        const int c = a + (b - a) / 2;
+        if (i < c) b = c, k = 2 * k;
+        else a = c, k = 2 * k + 1;
+    }
+    if (b - a < 4) return;
+    const double s = seam[(1ll << d) + k];
+    const double c0 = (d & 1) ? p0.y : p0.x, c1 = (d & 1) ? p1.y : p1.x;
+    const double dist = fmin(fabs(c0 - s), fabs(c1 - s));
+    const double len = fmax(fabs(p0.x - p1.x), fabs(p0.y - p1.y));
+    if (dist <= 3.0 * len)
+    {
+        const char* base = reinterpret_cast<const char*>(&R[r]);
+        asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(base));
+        asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(base + 32));
+    }
 }
 
 // Depths with at most this many nodes run one node per warp.
@@ -577,6 +768,11 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
     for (int d = D; d >= 0; --d)
     {
         const long long nodes = 1ll << d;
+        if (d <= kSeamDepth && b.seam && m >= (1 << 16))
+        {
+            k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, s>>>(b.recs, nrec, m, d, b.seam);
+            ++launch_counter();
+        }
         if (nodes <= kWarpNodes)
         {
             const unsigned g = (unsigned)((nodes * 32 + 127) / 128);

@@ -230,14 +230,37 @@ __global__ void k_iota(uint32_t* a, size_t m)
 // ---------------------------------------------------------------------------
 
 // side[point] = 1 if the point goes to the right child at depth d
-__global__ void k_split_mark(const uint32_t* __restrict__ S, uint8_t* __restrict__ side, int m, int d)
+// side[point] = 1 if the point goes to the right child at depth d. For the
+// upper depths (d <= kSeamDepth) the first point of every right child also
+// records the node's seam: the cut coordinate (x for even d, y for odd d)
+// that separates the children, used to prefetch the seam's records before
+// the node merges.
+__global__ void k_split_mark(const uint32_t* __restrict__ S, uint8_t* __restrict__ side, int m, int d,
+    const double2* __restrict__ ucoord, double* __restrict__ seam)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     int       lo, hi;
     const int dep = node_of(m, d, i, lo, hi);
     uint8_t   s = 0;
-    if (dep == d && hi - lo >= 4) s = (i >= lo + (hi - lo) / 2) ? 1 : 0;
+    if (dep == d && hi - lo >= 4)
+    {
+        const int mid = lo + (hi - lo) / 2;
+        s = (i >= mid) ? 1 : 0;
+        if (i == mid && d <= kSeamDepth)
+        {
+            long long k = 0;
+            int       a = 0, b = m;
+            for (int l = 0; l < d; ++l)
+            {
+                const int c = a + (b - a) / 2;
+                if (i < c) b = c, k = 2 * k;
+                else a = c, k = 2 * k + 1;
+            }
+            const double2 p = ucoord[S[i]];
+            seam[(1ll << d) + k] = (d & 1) ? p.y : p.x;
+        }
+    }
     side[S[i]] = s;
 }
 
@@ -354,7 +377,7 @@ void launch_split(PrepBuffers& b, int m, cudaStream_t s)
         int&      ocur = axis == 0 ? b.bcur : b.acur;
         uint32_t* O = axis == 0 ? b.B[ocur] : b.A[ocur];
         uint32_t* O2 = axis == 0 ? b.B[1 - ocur] : b.A[1 - ocur];
-        k_split_mark<<<grid_for(m, 256), 256, 0, s>>>(S, b.side, m, d);
+        k_split_mark<<<grid_for(m, 256), 256, 0, s>>>(S, b.side, m, d, b.ucoord, b.seam);
         ++launch_counter();
         scan_exclusive(SideOf{ O, b.side }, (size_t)m, b.uexcl, b.scratch, nullptr, s);
         k_split_scatter<<<grid_for(m, 256), 256, 0, s>>>(O, O2, b.side, b.uexcl, m, d);
