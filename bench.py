@@ -135,6 +135,17 @@ def cpu_threads():
     return max(1, min(64, os.cpu_count() or 1))
 
 
+def max_over_ranks(value, dist, device="cuda"):
+    """The slowest rank's value (replicas: the job ends when the last one
+    does). dist is torch.distributed or None."""
+    if dist is None:
+        return value
+    import torch
+    x = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
 def run_reference(args):
     """The reference arm: the CPU restatement of the reference's threaded
     batch driver, all host threads, on the same workload."""
@@ -237,11 +248,7 @@ def run_gb300(args):
     if dist:
         dist.barrier()
     ck = clocks.stop()
-    ms = statistics.mean(step_ms)
-    if dist:
-        x = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        ms = float(x.item())
+    ms = max_over_ranks(statistics.mean(step_ms), dist)
     value = ws * n / (ms / 1e3) / 1e6
 
     # end to end through qdt_execute with host buffers
@@ -256,11 +263,7 @@ def run_gb300(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
         if st != 0:
             raise RuntimeError("qdt_execute failed: %d" % st)
-    e2e = statistics.mean(e2e_ms)
-    if dist:
-        x = torch.tensor([e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        e2e = float(x.item())
+    e2e = max_over_ranks(statistics.mean(e2e_ms), dist)
     e2e_value = ws * n / (e2e / 1e3) / 1e6
     h2d = 16 * n
     d2h = 4 * 3 * 2 * m + 4 * n + 64

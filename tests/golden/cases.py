@@ -131,3 +131,36 @@ def make_large(spec) -> np.ndarray:
     if g == "line":
         return W.noisy_line(spec["n"], spec["seed"])
     raise ValueError(g)
+
+
+def mesh_cases():
+    """Handle operations after a batch call (qdt_verify.cpp's `examples`,
+    `insert` and `constraint` scenarios in spirit): (name, points, ops) with
+    ops a list of ("insert", x, y) and ("constraint", i, j)."""
+    out = []
+    sq = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0]])
+    out.append(("six_point_example", sq, [("insert", 0.5, 0.5), ("insert", 0.25, 0.75)]))
+    quad = np.array([[0.0, 0.0], [4.0, 0.0], [3.0, 1.0], [1.0, 1.0]])
+    out.append(("quad_constraint", quad, [("constraint", 0, 2), ("constraint", 0, 9), ("constraint", 1, 1),
+                                          ("constraint", 2, 0)]))
+    for s in range(12):
+        rng = np.random.default_rng(7000 + s)
+        n = int(rng.integers(5, 300))
+        if s % 3 == 0:
+            p = rng.random((n, 2))
+        elif s % 3 == 1:
+            p = rng.integers(0, 50, size=(n, 2)).astype(np.float64)
+        else:
+            p = np.round(rng.random((n, 2)) * 1000) / 8.0
+        ops = []
+        for _ in range(int(rng.integers(1, 40))):
+            if rng.random() < 0.5:
+                if s % 3 == 0:
+                    ops.append(("insert", float(rng.random() * 1.4 - 0.2), float(rng.random() * 1.4 - 0.2)))
+                else:
+                    q = p[int(rng.integers(0, n))] if rng.random() < 0.2 else rng.integers(-5, 55, size=2)
+                    ops.append(("insert", float(q[0]), float(q[1])))
+            else:
+                ops.append(("constraint", int(rng.integers(0, n + 5)), int(rng.integers(0, n + 5))))
+        out.append(("mixed_%d" % s, p, ops))
+    return out

@@ -85,6 +85,33 @@ def main():
     np.savez_compressed(os.path.join(HERE, "small_cases.npz"), **small)
     print("small cases:", len(small) // 3)
 
+    mesh = {}
+    for name, pts, ops in C.mesh_cases():
+        for par in (False, True):
+            with Q.Context(lib) as c:
+                st = c.execute(pts, parallel=par)
+                statuses = []
+                for op in ops:
+                    if op[0] == "insert":
+                        sti, idx = c.insert_point(op[1], op[2], parallel=par)
+                        statuses.append(int(sti))
+                        statuses.append(int(idx))
+                    else:
+                        statuses.append(int(c.insert_constraint(op[1], op[2])))
+                n = c.points_size()
+                tris = np.zeros((c.triangles_size(), 3), dtype=np.int64)
+                _ = run_ref  # bulk reader bound below
+                import ctypes as _ct
+                _dump.qdt_dump_triangles(c.ptr, tris.ctypes.data)
+                used = np.zeros(n, dtype=np.uint8)
+                _dump.qdt_dump_used(c.ptr, used.ctypes.data)
+            key = "%s/%s" % (name, "par" if par else "ser")
+            mesh[key + "/tris"] = O.canonical(tris).astype(np.int64)
+            mesh[key + "/status"] = np.array(statuses, dtype=np.int64)
+            mesh[key + "/used"] = used
+    np.savez_compressed(os.path.join(HERE, "mesh_cases.npz"), **mesh)
+    print("mesh cases:", len(mesh) // 3)
+
     out = {"canonical_form": "qdt_verify.cpp:408-427", "cases": []}
     for spec in C.large_specs():
         pts = C.make_large(spec)
