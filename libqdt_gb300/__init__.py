@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 GPU_SYMBOLS = ("qdtg_set_options", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
-               "qdtg_incircle", "qdtg_eval_predicates", "qdtg_version")
+               "qdtg_incircle", "qdtg_eval_predicates", "qdtg_unique_points_noalloc", "qdtg_version")
 
 
 class RunInfo(ctypes.Structure):
@@ -91,6 +91,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_incircle.restype = ctypes.c_int
     lib.qdtg_eval_predicates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_size_t, P]
     lib.qdtg_eval_predicates.restype = ctypes.c_int
+    lib.qdtg_unique_points_noalloc.argtypes = [P, ctypes.c_size_t, P, ctypes.POINTER(ctypes.c_size_t), P]
+    lib.qdtg_unique_points_noalloc.restype = ctypes.c_int
     lib.qdtg_version.argtypes = []
     lib.qdtg_version.restype = ctypes.c_char_p
     _lib = lib
