@@ -40,6 +40,13 @@ typedef struct qdtg_run_info
    stage_timing != 0 records CUDA events between the stages. */
 QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_timing);
 
+/* The largest subtree (in points, 4..1024) that the context builds in
+   on-chip shared memory before the levels above it run out of HBM; 0 builds
+   every level out of HBM. Default 256. Returns 1, or 0 for a NULL context,
+   a value out of range or no usable GPU. The triangulation does not depend
+   on it. */
+QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points);
+
 /* Fills *info for the last batch call of the context. Returns 1, or 0 when
    ptr or info is NULL. */
 QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info);
@@ -117,6 +124,67 @@ QDT_API int qdtg_eval_predicates(int kind, int mode, int on_device, const double
    array's device address; make that first call before any stream capture. */
 QDT_API qdt_status qdtg_unique_points_noalloc(const qdt_vec2d* d_pts, size_t n, uint32_t* d_rep,
     size_t* unique_points, void* cuda_stream);
+
+/* ------------------------------------------------------------------------
+   Many sets in one call. The reference triangulates one point set per
+   qdt_execute() call; a caller with thousands of independent sets (tiles,
+   frames, meshes of many parts) makes thousands of calls. A qdtg_batch
+   triangulates all of them in one GPU pipeline: set i is points
+   [offsets[i], offsets[i + 1]) of pts, and its result is the one
+   qdt_execute() gives for those points alone (triangles with indices local
+   to the set, the same representatives and distinct count).
+   ------------------------------------------------------------------------ */
+typedef struct qdtg_batch qdtg_batch;
+
+/* NULL when no GPU is usable. The batch keeps its device workspace, CUDA
+   stream and recorded CUDA graphs between calls. */
+QDT_API qdtg_batch* qdtg_batch_create(void);
+QDT_API void        qdtg_batch_destroy(qdtg_batch* b);
+
+/* Triangulates nsets sets of host points; offsets has nsets + 1 entries,
+   offsets[0] = 0, non-decreasing, offsets[nsets] = total points
+   (<= 100,000,000). Returns QDT_OK when the call ran (a set with a NaN or
+   infinite coordinate then has status QDT_ERR_NOT_FINITE and no result,
+   the others are complete), QDT_ERR_NULL_CONTEXT / QDT_ERR_NULL_ARGUMENT /
+   QDT_ERR_TOO_MANY_POINTS for bad arguments, QDT_ERR_OUT_OF_MEMORY or
+   QDT_ERR_INTERNAL otherwise (the batch is then empty). */
+QDT_API qdt_status qdtg_batch_execute(qdtg_batch* b, const qdt_vec2d* pts, const size_t* offsets, size_t nsets);
+
+/* The same for points resident on the device; the work waits for what is
+   queued on cuda_stream. Triangles and representatives stay on the device:
+   qdtg_batch_device_triangles(). */
+QDT_API qdt_status qdtg_batch_execute_device(qdtg_batch* b, const qdt_vec2d* d_pts, const size_t* offsets,
+    size_t nsets, void* cuda_stream);
+
+/* Results of the last call, per set. */
+QDT_API size_t     qdtg_batch_set_count(const qdtg_batch* b);
+QDT_API qdt_status qdtg_batch_set_status(const qdtg_batch* b, size_t set);
+/* Number of triangles of the set; *tris (if not NULL) points at 3 * count
+   host indices local to the set (NULL after qdtg_batch_execute_device). */
+QDT_API size_t qdtg_batch_triangles(const qdtg_batch* b, size_t set, const uint32_t** tris);
+QDT_API size_t qdtg_batch_unique_points(const qdtg_batch* b, size_t set);
+/* Representatives of the set's points (local indices), host memory. */
+QDT_API const uint32_t* qdtg_batch_rep(const qdtg_batch* b, size_t set);
+/* All triangles on the device: *d_tris = 3 * total indices (each set's
+   local), *d_offsets = nsets + 1 triangle offsets. Returns the total. */
+QDT_API size_t qdtg_batch_device_triangles(const qdtg_batch* b, const uint32_t** d_tris,
+    const uint32_t** d_offsets);
+/* Copies min(cap, total) device triangles to host memory out (3 indices
+   each) and, if offsets_out is not NULL, the nsets + 1 triangle offsets;
+   returns how many triangles it copied. */
+QDT_API size_t qdtg_batch_download_device_triangles(const qdtg_batch* b, uint32_t* out, size_t cap,
+    uint32_t* offsets_out);
+/* Counting of filter failures, per-stage timing (CUDA events), CUDA graph
+   replay of the launches after the distinct count (default on), and the
+   smallest merge (in points) that runs one node per warp instead of one
+   node per thread (0 keeps the current value; default 512). */
+QDT_API void qdtg_batch_set_options(qdtg_batch* b, int count_filter_failures, int stage_timing, int use_graphs,
+    int warp_min_points);
+/* The largest subtree (points, 4..1024; 0 = none) built in shared memory,
+   as qdtg_set_cell_points(). Returns 1, or 0 for a bad value. */
+QDT_API int   qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points);
+QDT_API int   qdtg_batch_get_run_info(const qdtg_batch* b, qdtg_run_info* info);
+QDT_API void* qdtg_batch_stream(const qdtg_batch* b);
 
 /* Library version string. */
 QDT_API const char* qdtg_version(void);

@@ -22,10 +22,15 @@ from .qdt_api import (QDT_OK, QDT_ERR_NULL_CONTEXT, QDT_ERR_NULL_ARGUMENT, QDT_E
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
-GPU_SYMBOLS = ("qdtg_set_options", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
+GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
-               "qdtg_incircle", "qdtg_eval_predicates", "qdtg_unique_points_noalloc", "qdtg_version")
+               "qdtg_incircle", "qdtg_eval_predicates", "qdtg_unique_points_noalloc", "qdtg_version",
+               "qdtg_batch_create", "qdtg_batch_destroy", "qdtg_batch_execute", "qdtg_batch_execute_device",
+               "qdtg_batch_set_count", "qdtg_batch_set_status", "qdtg_batch_triangles", "qdtg_batch_unique_points",
+               "qdtg_batch_rep", "qdtg_batch_device_triangles", "qdtg_batch_download_device_triangles",
+               "qdtg_batch_set_options", "qdtg_batch_set_cell_points", "qdtg_batch_get_run_info",
+               "qdtg_batch_stream")
 
 
 class RunInfo(ctypes.Structure):
@@ -69,6 +74,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     P = ctypes.c_void_p
     lib.qdtg_set_options.argtypes = [P, ctypes.c_int, ctypes.c_int]
     lib.qdtg_set_options.restype = None
+    lib.qdtg_set_cell_points.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_cell_points.restype = ctypes.c_int
     lib.qdtg_get_run_info.argtypes = [P, ctypes.POINTER(RunInfo)]
     lib.qdtg_get_run_info.restype = ctypes.c_int
     lib.qdtg_execute_device.argtypes = [P, P, ctypes.c_size_t, P]
@@ -95,6 +102,27 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_unique_points_noalloc.restype = ctypes.c_int
     lib.qdtg_version.argtypes = []
     lib.qdtg_version.restype = ctypes.c_char_p
+    S = ctypes.c_size_t
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    for name, args, res in (
+            ("qdtg_batch_create", [], P),
+            ("qdtg_batch_destroy", [P], None),
+            ("qdtg_batch_execute", [P, P, P, S], ctypes.c_int),
+            ("qdtg_batch_execute_device", [P, P, P, S, P], ctypes.c_int),
+            ("qdtg_batch_set_count", [P], S),
+            ("qdtg_batch_set_status", [P, S], ctypes.c_int),
+            ("qdtg_batch_triangles", [P, S, PP], S),
+            ("qdtg_batch_unique_points", [P, S], S),
+            ("qdtg_batch_rep", [P, S], P),
+            ("qdtg_batch_device_triangles", [P, PP, PP], S),
+            ("qdtg_batch_download_device_triangles", [P, P, S, P], S),
+            ("qdtg_batch_set_options", [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], None),
+            ("qdtg_batch_set_cell_points", [P, ctypes.c_int], ctypes.c_int),
+            ("qdtg_batch_get_run_info", [P, ctypes.POINTER(RunInfo)], ctypes.c_int),
+            ("qdtg_batch_stream", [P], P)):
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
     _lib = lib
     return lib
 
@@ -136,6 +164,9 @@ class Triangulation(qdt_api.Context):
         self.lib.qdtg_get_run_info(self.ptr, ctypes.byref(ri))
         return ri.as_dict()
 
+    def set_cell_points(self, cell_points: int) -> bool:
+        return self.lib.qdtg_set_cell_points(self.ptr, int(cell_points)) == 1
+
     def execute_device(self, d_ptr: int, n: int, stream: int = 0) -> int:
         return self.lib.qdtg_execute_device(self.ptr, d_ptr, n, stream or None)
 
@@ -153,6 +184,115 @@ class Triangulation(qdt_api.Context):
         if n:
             self.lib.qdtg_download_device_triangles(self.ptr, out.ctypes.data, n)
         return out
+
+
+class Batch:
+    """Many independent point sets triangulated by one GPU pipeline
+    (qdtg_batch_* of qdt_gpu.h). Set i of a call is points
+    offsets[i]:offsets[i+1]; its result equals qdt_execute() on those points
+    alone."""
+
+    def __init__(self, lib: ctypes.CDLL | None = None):
+        self.lib = lib or load()
+        self.ptr = self.lib.qdtg_batch_create()
+        if not self.ptr:
+            raise RuntimeError("qdtg_batch_create failed (no usable GPU)")
+        self._offsets = None
+
+    def close(self):
+        if self.ptr:
+            self.lib.qdtg_batch_destroy(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def offsets_of(sets) -> np.ndarray:
+        off = np.zeros(len(sets) + 1, dtype=np.uint64)
+        off[1:] = np.cumsum([len(s) for s in sets])
+        return off
+
+    def execute(self, pts, offsets) -> int:
+        """pts: (N, 2) float64 host array of all sets back to back."""
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 2)
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._offsets = off
+        return self.lib.qdtg_batch_execute(self.ptr, p.ctypes.data if p.size else None, off.ctypes.data,
+                                           len(off) - 1)
+
+    def execute_sets(self, sets) -> int:
+        off = self.offsets_of(sets)
+        pts = np.concatenate([np.asarray(s, dtype=np.float64).reshape(-1, 2) for s in sets]) if len(sets) else \
+            np.zeros((0, 2))
+        return self.execute(pts, off)
+
+    def execute_device(self, d_ptr: int, offsets, stream: int = 0) -> int:
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._offsets = off
+        return self.lib.qdtg_batch_execute_device(self.ptr, d_ptr or None, off.ctypes.data, len(off) - 1,
+                                                  stream or None)
+
+    def set_count(self) -> int:
+        return self.lib.qdtg_batch_set_count(self.ptr)
+
+    def status(self, i: int) -> int:
+        return self.lib.qdtg_batch_set_status(self.ptr, i)
+
+    def triangles(self, i: int) -> np.ndarray:
+        p = ctypes.c_void_p(0)
+        n = self.lib.qdtg_batch_triangles(self.ptr, i, ctypes.byref(p))
+        if n == 0 or not p.value:
+            return np.zeros((0, 3), dtype=np.uint32)
+        return np.ctypeslib.as_array((ctypes.c_uint32 * (3 * n)).from_address(p.value)).reshape(n, 3).copy()
+
+    def unique_points(self, i: int) -> int:
+        return self.lib.qdtg_batch_unique_points(self.ptr, i)
+
+    def rep(self, i: int) -> np.ndarray:
+        p = self.lib.qdtg_batch_rep(self.ptr, i)
+        n = int(self._offsets[i + 1] - self._offsets[i])
+        if not p or n == 0:
+            return np.zeros(0, dtype=np.uint32)
+        return np.ctypeslib.as_array((ctypes.c_uint32 * n).from_address(p)).copy()
+
+    def device_triangles(self):
+        t, o = ctypes.c_void_p(0), ctypes.c_void_p(0)
+        n = self.lib.qdtg_batch_device_triangles(self.ptr, ctypes.byref(t), ctypes.byref(o))
+        return n, t.value, o.value
+
+    def download_device_triangles(self):
+        """All triangles (total, 3) and the per-set triangle offsets."""
+        total, _, _ = self.device_triangles()
+        tri = np.zeros((total, 3), dtype=np.uint32)
+        off = np.zeros(self.set_count() + 1, dtype=np.uint32)
+        self.lib.qdtg_batch_download_device_triangles(self.ptr, tri.ctypes.data if total else None, total,
+                                                      off.ctypes.data)
+        return tri, off
+
+    def set_options(self, count_filter_failures=False, stage_timing=False, use_graphs=True, warp_min_points=0):
+        self.lib.qdtg_batch_set_options(self.ptr, int(count_filter_failures), int(stage_timing), int(use_graphs),
+                                        int(warp_min_points))
+
+    def run_info(self) -> dict:
+        ri = RunInfo()
+        self.lib.qdtg_batch_get_run_info(self.ptr, ctypes.byref(ri))
+        return ri.as_dict()
+
+    def set_cell_points(self, cell_points: int) -> bool:
+        return self.lib.qdtg_batch_set_cell_points(self.ptr, int(cell_points)) == 1
+
+    def stream(self) -> int:
+        return self.lib.qdtg_batch_stream(self.ptr) or 0
 
 
 def eval_predicates(kind: str, coords, mode: str = "full", device: bool = False) -> np.ndarray:

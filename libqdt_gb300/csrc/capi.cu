@@ -4,6 +4,7 @@
 #include <cmath>
 #include <new>
 
+#include "common.cuh"
 #include "context.hpp"
 #include "qdt.h"
 #include "qdt_gpu.h"
@@ -335,6 +336,16 @@ QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_t
     if (qdtg::ensure_engine(*c) != QDT_OK) return;
     c->engine->set_count_filter(count_filter_failures != 0);
     c->engine->set_timing(stage_timing != 0);
+}
+
+QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points)
+{
+    Context* c = ctx(ptr);
+    if (!c) return 0;
+    if (cell_points != 0 && (cell_points < 4 || cell_points > qdtg::kCellMax)) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_cell_points(cell_points);
+    return 1;
 }
 
 QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)

@@ -66,6 +66,10 @@ struct DevStatus
 // seam records are prefetched into L2 before they merge.
 constexpr int kSeamDepth = 10;
 
+// Largest cell (points) built in shared memory: 6 * kCellMax half-edge ids
+// fit in the 16-bit ids of the cell's records.
+constexpr int kCellMax = 1024;
+
 // The Dwyer split tree depends only on the number m of distinct points: the
 // root covers [0, m); a node [lo, hi) of at least 4 points splits at
 // lo + (hi - lo) / 2 (reference builder.hxx:306-308). Depth d, heap-style

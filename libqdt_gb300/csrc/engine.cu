@@ -222,6 +222,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     const size_t m = hs->words[0];
     info_.unique_points = m;
     b.count_filter = count_filter_ ? 1 : 0;
+    b.cell_points = cell_points_;
     if (m >= 3)
     {
         launch_frames(p, m, s);

@@ -108,6 +108,8 @@ public:
     cudaStream_t    stream() const { return stream_; }
     void            set_count_filter(bool on) { count_filter_ = on; }
     void            set_timing(bool on) { timing_ = on; }
+    void            set_cell_points(int c) { cell_points_ = c; }
+    int             cell_points() const { return cell_points_; }
 
 private:
     Engine() = default;
@@ -120,6 +122,7 @@ private:
     RunInfo         info_;
     bool            count_filter_ = false;
     bool            timing_ = false;
+    int             cell_points_ = 0;
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -51,6 +51,7 @@ struct BuildBuffers
     DevStatus*     status = nullptr;
     const double*  seam = nullptr;      // cut coordinates of the upper nodes (PrepBuffers::seam)
     int            count_filter = 0;    // count filter failures in status
+    int            cell_points = 0;     // largest cell built in shared memory (0: no cells)
 };
 
 size_t sort_count_words(size_t n);

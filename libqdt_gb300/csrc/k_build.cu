@@ -24,6 +24,7 @@
 // * every record access is bounds-checked and every loop has an iteration
 //   guard; a violation sets a device status bit and ends the thread, and the
 //   host reports QDT_ERR_INTERNAL. No trap, no hang.
+#include "builder.cuh"
 #include "common.cuh"
 #include "engine_kernels.hpp"
 #include "predicates.cuh"
@@ -31,618 +32,7 @@
 
 namespace qdtg {
 
-__device__ __forceinline__ int sym(int e) { return e ^ 1; }
 
-// reference builder.hxx:71-76
-__device__ __forceinline__ bool less_frame(double2 a, double2 b, int frame)
-{
-    if (frame == 0) return a.x < b.x || (a.x == b.x && a.y < b.y);
-    return a.y < b.y || (a.y == b.y && a.x > b.x);
-}
-
-__device__ __forceinline__ bool ccw(double2 a, double2 b, double2 c, PredCounters* pc)
-{
-    return orient2d_sign(a.x, a.y, b.x, b.y, c.x, c.y, pc) > 0;
-}
-
-struct Builder
-{
-    Rec*          R;
-    int           nrec;
-    DevStatus*    st;
-    PredCounters* pc;
-    int           fhead, ftail;
-    bool          bad;
-
-    __device__ __forceinline__ void fail(unsigned bit)
-    {
-        if (!bad) atomicOr(&st->flags, bit);
-        bad = true;
-    }
-    __device__ __forceinline__ int chk(int e)
-    {
-        // one unsigned compare: negative ids wrap to large values
-        if ((unsigned)e >= 2u * (unsigned)nrec)
-        {
-            fail(ST_BAD_INDEX);
-            return 0;
-        }
-        return e;
-    }
-
-    __device__ __forceinline__ int onext(int e)
-    {
-        e = chk(e);
-        return R[e >> 1].next[e & 1];
-    }
-    __device__ __forceinline__ int oprev(int e)
-    {
-        e = chk(e);
-        return R[e >> 1].prev[e & 1];
-    }
-    __device__ __forceinline__ int org(int e)
-    {
-        e = chk(e);
-        return R[e >> 1].org[e & 1];
-    }
-    __device__ __forceinline__ double2 porg(int e)
-    {
-        e = chk(e);
-        return R[e >> 1].p[e & 1];
-    }
-    __device__ __forceinline__ int     dest(int e) { return org(sym(e)); }
-    __device__ __forceinline__ double2 pdest(int e) { return porg(sym(e)); }
-    __device__ __forceinline__ int     lnext(int e) { return oprev(sym(e)); }
-    __device__ __forceinline__ int     rprev(int e) { return onext(sym(e)); }
-
-    // the ids written here were all read through onext/oprev just before,
-    // which checked them
-    __device__ __forceinline__ void set_next(int e, int v)
-    {
-        if (!bad) R[e >> 1].next[e & 1] = v;
-    }
-    __device__ __forceinline__ void set_prev(int e, int v)
-    {
-        if (!bad) R[e >> 1].prev[e & 1] = v;
-    }
-
-    // free list of the node (records of the subtree that are not in use)
-    // The link of the popped record is needed only by the next alloc(), so
-    // nothing waits for that load here; the tail is settled by
-    // settle_tail() when the node is done (an emptied list has no tail).
-    __device__ int alloc()
-    {
-        const int k = fhead;
-        if (k < 0 || k >= nrec)
-        {
-            fail(ST_POOL_EMPTY);
-            return -1;
-        }
-        fhead = R[k].link;
-        return k;
-    }
-    __device__ void release(int k)
-    {
-        if (bad) return;
-        R[k].org[0] = -1;
-        R[k].link = fhead;
-        if (fhead < 0) ftail = k;
-        fhead = k;
-    }
-    __device__ void settle_tail()
-    {
-        if (fhead < 0) ftail = -1;
-    }
-
-    // reference builder.hxx:131-142: a new edge, alone in the rings of both
-    // its origins, with both origins (and their coordinates) set at once
-    __device__ int make_edge(int o0, int o1, double2 p0, double2 p1)
-    {
-        if (bad) return 0;
-        const int k = alloc();
-        if (k < 0) return 0;
-        const int e = 2 * k;
-        Rec&      r = R[k];
-        *reinterpret_cast<int4*>(&r.next[0]) = make_int4(e, e + 1, e, e + 1);
-        *reinterpret_cast<int4*>(&r.org[0]) = make_int4(o0, o1, -1, 0);
-        r.p[0] = p0;
-        r.p[1] = p1;
-        return e;
-    }
-
-    // splice(e, x) of an edge e alone in its ring (builder.hxx:144-149):
-    // e follows x counter-clockwise around their common origin
-    __device__ void insert_after(int x, int e)
-    {
-        const int n = onext(x);
-        set_next(e, n);
-        set_prev(e, x);
-        set_prev(n, e);
-        set_next(x, e);
-    }
-    // splice(e, oprev(e)): e leaves the ring around its origin
-    __device__ void remove(int e)
-    {
-        const int p = oprev(e), n = onext(e);
-        set_next(p, n);
-        set_prev(n, p);
-    }
-
-    // reference builder.hxx:151-159
-    __device__ int connect(int a, int b)
-    {
-        const int e = make_edge(dest(a), org(b), pdest(a), porg(b));
-        if (bad) return 0;
-        insert_after(lnext(a), e);
-        insert_after(b, sym(e));
-        return e;
-    }
-
-    // reference builder.hxx:161-166
-    __device__ void delete_edge(int e)
-    {
-        e = chk(e);
-        remove(e);
-        remove(sym(e));
-        release(e >> 1);
-    }
-
-    // reference builder.hxx:171-175: false when two of the vertices coincide
-    __device__ bool in_circle(int a, double2 pa, int b, double2 pb, int c, double2 pc_, int d, double2 pd)
-    {
-        if (a == d || b == d || c == d || a == b || a == c || b == c) return false;
-        return incircle_sign(pa.x, pa.y, pb.x, pb.y, pc_.x, pc_.y, pd.x, pd.y, pc) > 0;
-    }
-
-    // reference builder.hxx:177-201. The leaf's points are V[lo, hi), already
-    // in the order of the frame; its records are [3 lo, 3 hi).
-    __device__ void leaf(int lo, int hi, const double2* __restrict__ V, int& le, int& re)
-    {
-        const int r0 = 3 * lo, r1 = 3 * hi;
-        for (int k = r0; k < r1; ++k)
-            *reinterpret_cast<int4*>(&R[k].org[0]) = make_int4(-1, -1, k + 1 < r1 ? k + 1 : -1, 0);
-        fhead = r0;
-        ftail = r1 - 1;
-        const int     n = hi - lo, s1 = lo, s2 = lo + 1;
-        const double2 p1 = V[s1], p2 = V[s2];
-        if (n == 2)
-        {
-            const int a = make_edge(s1, s2, p1, p2);
-            le = a;
-            re = sym(a);
-            return;
-        }
-        const int     s3 = lo + 2;
-        const double2 p3 = V[s3];
-        const int     a = make_edge(s1, s2, p1, p2), b = make_edge(s2, s3, p2, p3);
-        insert_after(sym(a), b);
-        const int o = orient2d_sign(p1.x, p1.y, p2.x, p2.y, p3.x, p3.y, pc);
-        if (o > 0)
-        {
-            connect(b, a);
-            le = a;
-            re = sym(b);
-            return;
-        }
-        if (o < 0)
-        {
-            const int c = connect(b, a);
-            le = sym(c);
-            re = c;
-            return;
-        }
-        le = a;
-        re = sym(b);
-    }
-
-    // lower common tangent (builder.hxx:253-261)
-    __device__ int tangent(int& ldo, int& ldi, int& rdi, int& rdo, int lim)
-    {
-        int it = 0;
-        for (;;)
-        {
-            if (bad) return 0;
-            if (++it > lim)
-            {
-                fail(ST_GUARD);
-                return 0;
-            }
-            // leftOf(org(rdi), ldi), then rightOf(org(ldi), rdi)
-            const double2 prdi = porg(rdi), pldi = porg(ldi);
-            if (ccw(prdi, pldi, pdest(ldi), pc)) ldi = lnext(ldi);
-            else if (ccw(pldi, pdest(rdi), prdi, pc)) rdi = rprev(rdi);
-            else break;
-        }
-        const int basel = connect(sym(rdi), ldi);
-        if (org(ldi) == org(ldo)) ldo = sym(basel);
-        if (org(rdi) == org(rdo)) rdo = basel;
-        return basel;
-    }
-
-    // reference builder.hxx:251-285 (with the scans :205-249 in line)
-    __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
-    {
-        int basel = tangent(ldo, ldi, rdi, rdo, lim);
-        int it = 0;
-        for (;;)
-        {
-            if (bad) return;
-            if (++it > lim)
-            {
-                fail(ST_GUARD);
-                return;
-            }
-            const int     bo = org(basel), bd = dest(basel);
-            const double2 pbo = porg(basel), pbd = pdest(basel);
-            // left candidate (builder.hxx:205-226)
-            int     lc = onext(sym(basel));
-            int     lcd = dest(lc);
-            double2 plcd = pdest(lc);
-            bool    lv = ccw(plcd, pbd, pbo, pc);
-            if (lv)
-            {
-                bool deleted = false;
-                int  j = 0;
-                for (;;)
-                {
-                    const int     t = onext(lc);
-                    const int     td = dest(t);
-                    const double2 ptd = pdest(t);
-                    if (!in_circle(bd, pbd, bo, pbo, lcd, plcd, td, ptd)) break;
-                    if (bad || ++j > lim)
-                    {
-                        fail(ST_GUARD);
-                        return;
-                    }
-                    delete_edge(lc);
-                    lc = t;
-                    lcd = td;
-                    plcd = ptd;
-                    deleted = true;
-                }
-                if (deleted) lv = ccw(plcd, pbd, pbo, pc);
-            }
-            // right candidate (builder.hxx:228-249)
-            int     rc = oprev(basel);
-            int     rcd = dest(rc);
-            double2 prcd = pdest(rc);
-            bool    rv = ccw(prcd, pbd, pbo, pc);
-            if (rv)
-            {
-                bool deleted = false;
-                int  j = 0;
-                for (;;)
-                {
-                    const int     t = oprev(rc);
-                    const int     td = dest(t);
-                    const double2 ptd = pdest(t);
-                    if (!in_circle(bd, pbd, bo, pbo, rcd, prcd, td, ptd)) break;
-                    if (bad || ++j > lim)
-                    {
-                        fail(ST_GUARD);
-                        return;
-                    }
-                    delete_edge(rc);
-                    rc = t;
-                    rcd = td;
-                    prcd = ptd;
-                    deleted = true;
-                }
-                if (deleted) rv = ccw(prcd, pbd, pbo, pc);
-            }
-            if (!lv && !rv) break;
-            if (!lv || (rv && in_circle(lcd, plcd, bd, pbd, bo, pbo, rcd, prcd)))
-                basel = connect(rc, sym(basel));
-            else
-                basel = connect(sym(basel), sym(lc));
-        }
-        out_l = ldo;
-        out_r = rdo;
-    }
-
-    // reference builder.hxx:287-301
-    __device__ int hull_walk(int e, int frame, bool want_max, int lim)
-    {
-        for (int it = 0;; ++it)
-        {
-            if (bad) return e;
-            if (it > lim)
-            {
-                fail(ST_GUARD);
-                return e;
-            }
-            const int     nx = rprev(e);
-            const int     pv = sym(oprev(e));
-            const double2 pe = porg(e);
-            const double2 pn = porg(nx);
-            if (want_max ? less_frame(pe, pn, frame) : less_frame(pn, pe, frame))
-            {
-                e = nx;
-                continue;
-            }
-            const double2 pp = porg(pv);
-            if (want_max ? less_frame(pe, pp, frame) : less_frame(pp, pe, frame))
-            {
-                e = pv;
-                continue;
-            }
-            return e;
-        }
-    }
-};
-
-// ---------------------------------------------------------------------------
-// Warp-cooperative merge (the upper levels)
-// ---------------------------------------------------------------------------
-//
-// The same merge as Builder::merge, organised around a window of candidates
-// that the warp loads once per bubble step:
-//
-// * left lanes 0..15 walk the ring of bd counter-clockwise from
-//   c_0 = onext(sym(basel)), right lanes 16..31 the ring of bo clockwise from
-//   r_0 = oprev(basel), loading kWin+1 records (c_0..c_4); every lane of a
-//   side loads the same records, so each load is one broadcast transaction;
-// * lanes 0..3 and 16..19 evaluate validE(c_j) and inCircle(bd, bo,
-//   dest(c_j), dest(c_j+1)); lanes 4..11 and 20..27 evaluate the final choice
-//   inCircle(dest(c_a), bd, bo, dest(r_b)) for all 16 (a, b): one wave of
-//   predicates, one warp instruction stream for all of them;
-// * ballots give what the reference's sequential loop (builder.hxx:205-283)
-//   computes one test after the other: how many candidates each scan
-//   deletes (up to the first failing in-circle test), lv, rv and the choice.
-//   The two scans touch disjoint edges (builder.hxx:203-204), so evaluating
-//   them together decides the same;
-// * the map edits need no further loads: the deleted candidates c_0..c_dl-1
-//   are a run of consecutive edges in bd's ring (one link update), and each
-//   one's far end leaves the ring of its other origin using the prev/next of
-//   its own record, already in the window -- one lane per deleted edge; the
-//   new base edge is inserted between neighbours that the window also holds.
-//   The free list takes the deleted records in the reference's order.
-// A scan that deletes its whole window goes on in another pass, without
-// re-testing validity (builder.hxx:216-222). Record indices are clamped to
-// the pool, so no access leaves it; the loops are bounded by guards.
-constexpr int kWin = 4;
-
-struct Ent
-{
-    int     e;    // half-edge
-    int     nx;   // its successor along the scan (onext for the left side, oprev for the right)
-    int     d;    // dest(e)
-    int     fp;   // oprev(sym(e)): neighbours of the far end in the ring of dest(e)
-    int     fn;   // onext(sym(e))
-    double2 p;    // coordinates of dest(e)
-};
-
-__device__ __forceinline__ Ent load_ent(const Rec* __restrict__ R, int e, int nrec, bool left)
-{
-    const int  k = (int)min((unsigned)(e >> 1), (unsigned)(nrec - 1));
-    const int  s = e & 1;
-    const int4 np = *reinterpret_cast<const int4*>(&R[k].next[0]);   // next0 next1 prev0 prev1
-    const int2 og = *reinterpret_cast<const int2*>(&R[k].org[0]);
-    Ent        x;
-    x.e = e;
-    x.nx = left ? (s ? np.y : np.x) : (s ? np.w : np.z);
-    x.d = s ? og.x : og.y;
-    x.fp = s ? np.z : np.w;
-    x.fn = s ? np.x : np.y;
-    x.p = R[k].p[s ^ 1];
-    return x;
-}
-
-__device__ __forceinline__ Rec& recof(Rec* R, int e, int nrec)
-{
-    return R[min((unsigned)(e >> 1), (unsigned)(nrec - 1))];
-}
-__device__ __forceinline__ void st_next(Rec* R, int e, int v, int nrec) { recof(R, e, nrec).next[e & 1] = v; }
-__device__ __forceinline__ void st_prev(Rec* R, int e, int v, int nrec) { recof(R, e, nrec).prev[e & 1] = v; }
-
-__device__ __forceinline__ double2 shfl_d2(double2 v, int src)
-{
-    return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-}
-
-__device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
-{
-    const unsigned FULL = 0xffffffffu;
-    Rec* const     R = B.R;
-    const int      nrec = B.nrec;
-    const int      lane = threadIdx.x & 31;
-    const bool     left = lane < 16;
-    const int      j = lane & 15;
-    const bool     slot = j < kWin;
-    const bool     combo = j >= 4 && j < 12;
-    const int      q = left ? (j - 4) : (j + 4);   // combo index 0..15 = 4 a + b
-    const int      ca = q >> 2, rb = q & 3;
-    const int      jj = slot ? j : 0;               // window slot this lane keeps
-
-    int basel = 0;
-    if (lane == 0) basel = B.tangent(ldo, ldi, rdi, rdo, lim);
-    __syncwarp();
-    basel = __shfl_sync(FULL, basel, 0);
-    bool bad = __shfl_sync(FULL, (int)B.bad, 0) != 0;
-    // free list: head and the link of the head
-    int fhead = __shfl_sync(FULL, B.fhead, 0), ftail = __shfl_sync(FULL, B.ftail, 0);
-    int flink = (fhead >= 0 && !bad) ? recof(R, 2 * fhead, nrec).link : -1;
-    // the base edge, its endpoints and the starts of both windows
-    int     bo = 0, bd = 0, lstart = 0, rstart = 0;
-    double2 pbo = make_double2(0, 0), pbd = pbo;
-    if (!bad)
-    {
-        bo = B.org(basel);
-        bd = B.dest(basel);
-        pbo = B.porg(basel);
-        pbd = B.pdest(basel);
-        lstart = B.onext(sym(basel));
-        rstart = B.oprev(basel);
-    }
-    int it = 0;
-    while (!bad)
-    {
-        if (++it > lim)
-        {
-            if (lane == 0) B.fail(ST_GUARD);
-            break;
-        }
-        bool cont_l = false, cont_r = false, lv = false, rv = false, choice = false;
-        int  lcE = 0, lcD = 0, lcFn = 0, rcE = 0, rcD = 0, rcFp = 0;
-        double2 lcP = pbo, rcP = pbo;
-        for (int pass = 0;; ++pass)
-        {
-            if (pass > lim)
-            {
-                if (lane == 0) B.fail(ST_GUARD);
-                bad = true;
-                break;
-            }
-            // --- the window: kWin + 1 records along this side's ring
-            Ent cur = load_ent(R, left ? lstart : rstart, nrec, left);
-            Ent mine = cur, succ = cur;
-#pragma unroll
-            for (int i = 1; i <= kWin; ++i)
-            {
-                const Ent nx = load_ent(R, cur.nx, nrec, left);
-                if (i == jj) mine = nx;
-                if (i == jj + 1) succ = nx;
-                cur = nx;
-            }
-            // --- one wave of predicates
-            const int     src_a = combo ? ca : 0, src_b = combo ? 16 + rb : 16;
-            const int     ad = __shfl_sync(FULL, mine.d, src_a), bdst = __shfl_sync(FULL, mine.d, src_b);
-            const double2 pa = shfl_d2(mine.p, src_a), pb = shfl_d2(mine.p, src_b);
-            const bool valid = slot && ccw(mine.p, pbd, pbo, B.pc);
-            // one in-circle call for both roles, so the lanes share one
-            // instruction stream: slot (bd, bo, dest c_j, dest c_j+1),
-            // choice (dest c_a, bd, bo, dest r_b)
-            const int     ia = slot ? bd : ad, ib = slot ? bo : bd, ic = slot ? mine.d : bo, id = slot ? succ.d : bdst;
-            const double2 qa = slot ? pbd : pa, qb = slot ? pbo : pbd, qc = slot ? mine.p : pbo,
-                          qd = slot ? succ.p : pb;
-            const bool inc = (slot || combo) && B.in_circle(ia, qa, ib, qb, ic, qc, id, qd);
-            const unsigned vm = __ballot_sync(FULL, valid), im = __ballot_sync(FULL, inc);
-            const unsigned vl = vm & 0xFu, il = im & 0xFu, vr = (vm >> 16) & 0xFu, ir = (im >> 16) & 0xFu;
-            const unsigned zl = ~il & 0xFu, zr = ~ir & 0xFu;
-            const int      dl = (cont_l || (vl & 1u)) ? (zl ? __ffs(zl) - 1 : kWin) : 0;
-            const int      dr = (cont_r || (vr & 1u)) ? (zr ? __ffs(zr) - 1 : kWin) : 0;
-            // the candidate each scan stops at: slot dl (slot kWin is the
-            // successor of slot kWin - 1)
-            const int  srcL = min(dl, kWin - 1), srcR = 16 + min(dr, kWin - 1);
-            const bool overL = dl == kWin, overR = dr == kWin;
-            const int  stopL = overL ? __shfl_sync(FULL, succ.e, srcL) : __shfl_sync(FULL, mine.e, srcL);
-            const int  stopR = overR ? __shfl_sync(FULL, succ.e, srcR) : __shfl_sync(FULL, mine.e, srcR);
-            // --- deletions: far ends (one lane per deleted edge), the
-            // near-end rings, and the free list in the reference's order
-            const int prevrec = __shfl_up_sync(FULL, mine.e >> 1, 1);
-            const int lastL = dl > 0 ? __shfl_sync(FULL, mine.e >> 1, dl - 1) : -1;
-            const int lastR = dr > 0 ? __shfl_sync(FULL, mine.e >> 1, 16 + dr - 1) : -1;
-            const int firstL = __shfl_sync(FULL, mine.e >> 1, 0), firstR = __shfl_sync(FULL, mine.e >> 1, 16);
-            const bool del = slot && j < (left ? dl : dr);
-            if (del)
-            {
-                st_next(R, mine.fp, mine.fn, nrec);
-                st_prev(R, mine.fn, mine.fp, nrec);
-                Rec&      r = recof(R, mine.e, nrec);
-                const int below = (j > 0) ? prevrec : (left ? fhead : (dl > 0 ? lastL : fhead));
-                r.org[0] = -1;
-                r.link = below;
-            }
-            if (lane == 0 && dl > 0)
-            {
-                st_next(R, sym(basel), stopL, nrec);
-                st_prev(R, stopL, sym(basel), nrec);
-            }
-            if (lane == 16 && dr > 0)
-            {
-                st_prev(R, basel, stopR, nrec);
-                st_next(R, stopR, basel, nrec);
-            }
-            if (dl + dr > 0)
-            {
-                const int old = fhead;
-                const int newhead = dr > 0 ? lastR : lastL;
-                if (old < 0) ftail = dl > 0 ? firstL : firstR;
-                flink = dr > 1 ? __shfl_sync(FULL, mine.e >> 1, 16 + dr - 2)
-                               : (dr == 1 ? (dl > 0 ? lastL : old) : (dl > 1 ? __shfl_sync(FULL, mine.e >> 1, dl - 2) : old));
-                fhead = newhead;
-            }
-            lstart = stopL;
-            rstart = stopR;
-            __syncwarp();
-            if (overL || overR)
-            {
-                cont_l = cont_l || overL;
-                cont_r = cont_r || overR;
-                continue;
-            }
-            lv = (vl >> dl) & 1u;
-            rv = (vr >> dr) & 1u;
-            lcE = stopL;
-            lcD = __shfl_sync(FULL, mine.d, srcL);
-            lcP = shfl_d2(mine.p, srcL);
-            lcFn = __shfl_sync(FULL, mine.fn, srcL);
-            rcE = stopR;
-            rcD = __shfl_sync(FULL, mine.d, srcR);
-            rcP = shfl_d2(mine.p, srcR);
-            rcFp = __shfl_sync(FULL, mine.fp, srcR);
-            const int ql = dl * 4 + dr;
-            const int qlane = ql < 8 ? 4 + ql : 20 + (ql - 8);
-            choice = (im >> qlane) & 1u;
-            break;
-        }
-        if (bad || (!lv && !rv)) break;
-        // --- the new base edge (builder.hxx:279-282), from window values only
-        const bool take_r = !lv || (rv && choice);
-        const int  k = fhead;
-        if (k < 0 || k >= nrec)
-        {
-            if (lane == 0) B.fail(ST_POOL_EMPTY);
-            break;
-        }
-        fhead = flink;
-        const int e = 2 * k;
-        int       o0, o1, x0, n0, x1, n1;   // e after x0 (before n0); sym(e) after x1 (before n1)
-        double2   p0, p1;
-        if (take_r)
-        {
-            // connect(rc, sym(basel)): from dest(rc) to bd
-            o0 = rcD, p0 = rcP, o1 = bd, p1 = pbd;
-            x0 = rcFp, n0 = sym(rcE);
-            x1 = sym(basel), n1 = lstart;
-        }
-        else
-        {
-            // connect(sym(basel), sym(lc)): from bo to dest(lc)
-            o0 = bo, p0 = pbo, o1 = lcD, p1 = lcP;
-            x0 = rstart, n0 = basel;
-            x1 = sym(lcE), n1 = lcFn;
-        }
-        if (lane == 0)
-        {
-            Rec& r = R[k];
-            *reinterpret_cast<int4*>(&r.next[0]) = make_int4(n0, n1, x0, x1);
-            *reinterpret_cast<int4*>(&r.org[0]) = make_int4(o0, o1, -1, 0);
-            r.p[0] = p0;
-            r.p[1] = p1;
-            st_next(R, x0, e, nrec);
-            st_prev(R, n0, e, nrec);
-            st_next(R, x1, e + 1, nrec);
-            st_prev(R, n1, e + 1, nrec);
-        }
-        // the next step's base edge and window starts
-        basel = e;
-        bo = o0, pbo = p0, bd = o1, pbd = p1;
-        lstart = n1;   // onext(sym(e))
-        rstart = x0;   // oprev(e)
-        if (fhead >= 0) flink = recof(R, 2 * fhead, nrec).link;
-        __syncwarp();
-    }
-    if (lane == 0)
-    {
-        B.fhead = fhead;
-        B.ftail = ftail;
-    }
-    out_l = __shfl_sync(FULL, ldo, 0);
-    out_r = __shfl_sync(FULL, rdo, 0);
-}
-
-constexpr unsigned kFatal = ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX;
 
 // One depth of the tree: leaves of that depth are built, internal nodes merge
 // their children's results (written by the previous launch). WARP: one node
@@ -758,13 +148,41 @@ __global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int
     }
 }
 
+// The cells of depth dc, one warp each (build_cell).
+__global__ void __launch_bounds__(kCellBlockWarps * 32) k_build_cells(Rec* __restrict__ R,
+    const double2* __restrict__ V, NodeOut* __restrict__ out, int m, int dc, int C, DevStatus* st, int count)
+{
+    extern __shared__ __align__(16) char cell_smem[];
+    const int       w = threadIdx.x >> 5;
+    const long long k = (long long)blockIdx.x * (blockDim.x >> 5) + w;
+    if (k >= (1ll << dc)) return;
+    const unsigned flags = __shfl_sync(0xffffffffu, *(volatile unsigned*)&st->flags, 0);
+    if (flags & kFatal) return;
+    int lo, hi;
+    if (!node_range(m, dc, k, lo, hi) || hi - lo > C) return;
+    build_cell(cell_smem + w * cell_smem_bytes(C), V, R, lo, hi, dc, st, count ? &st->pc : nullptr, out + k);
+}
+
 // Depths with at most this many nodes run one node per warp.
 constexpr long long kWarpNodes = 1 << 12;
 
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 {
-    const int D = split_levels(m);
     const int nrec = 3 * m;
+    int       D = split_levels(m);
+    const int C = b.cell_points;
+    if (C >= 4 && C <= kCellMax)
+    {
+        // the bottom of the tree in shared-memory cells, then the levels above
+        const int dc = cell_depth(m, C);
+        const int warps = cell_block_warps(C);
+        const int bytes = warps * cell_smem_bytes(C);
+        cudaFuncSetAttribute(k_build_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        const unsigned g = (unsigned)(((1ll << dc) + warps - 1) / warps);
+        k_build_cells<<<g, warps * 32, bytes, s>>>(b.recs, b.V, b.node[dc & 1], m, dc, C, b.status, b.count_filter);
+        ++launch_counter();
+        D = dc - 1;
+    }
     for (int d = D; d >= 0; --d)
     {
         const long long nodes = 1ll << d;

@@ -120,6 +120,21 @@ def test_random_sets_equal_oracle(lib):
         assert np.array_equal(rep, o.rep)
 
 
+def test_cell_sizes_same_result(lib):
+    """The shared-memory cells are a schedule, not a different algorithm: the
+    triangulation is the same for every cell size, none included."""
+    inputs = [W.uniform(60000, 31), W.lattice_with_duplicates(128, 0.02, 32), W.unit_circle(5000, 33),
+              W.noisy_line(20000, 34), W.gaussian_mixture(30000, 8, 35), W.uniform(5, 36), W.uniform(1100, 37)]
+    for p in inputs:
+        want = O.canonical(O.triangulate(p).tris)
+        with G.Triangulation(lib) as t:
+            for c in (0, 4, 5, 17, 64, 256, 1024):
+                assert t.set_cell_points(c)
+                assert t.execute(p) == 0
+                assert np.array_equal(O.canonical(t.triangles_array()), want), (p.shape, c)
+            assert not t.set_cell_points(3) and not t.set_cell_points(1025)
+
+
 @pytest.mark.parametrize("name", ["gauss_300k", "circle_100k", "line_1m", "lattice_512"])
 def test_exact_checker_zero_violations(lib, name):
     pts = {"gauss_300k": lambda: W.gaussian_mixture(300000, 64, 5),
