@@ -309,12 +309,134 @@ def run_gb300(args):
         cb = n / statistics.median(times) / 1e6
         line["cpu_baseline"] = {"value": round(cb, 4), "unit": UNIT, "cores": nt, "kind": "port",
                                 "sample": "%d full runs of the workload, threaded driver" % len(times)}
+    t.close()
+    del d_pts
+    torch.cuda.empty_cache()
+    if rank == 0 and ws == 1:
+        legs = [x for x in args.legs.split(",") if x]
+        if "batched" in legs:
+            line["batched"] = run_batched_leg(lib, args, flush)
+        if "serving" in legs:
+            line["serving"] = run_serving_leg(lib, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
-    t.close()
     return 0
+
+
+def run_batched_leg(lib, args, flush):
+    """Config B: 4,096 independent sets (sizes log-uniform in [16, 65536],
+    unit square or disk, 10% snapped to a 256 grid) in one many-set call,
+    against the plain path called once per set. Device-resident timing with
+    CUDA events on the batch's stream (L2 flushed between steps), end to end
+    through qdtg_batch_execute with host buffers, and the plain qdt_execute
+    loop over the sets (wall clock, one pass)."""
+    import numpy as np
+    import torch
+
+    import libqdt_gb300 as G
+    from libqdt_gb300 import workloads as W
+    from oracle import delaunay_check as D
+
+    sets = W.many_sets(count=4096, lo=16, hi=65536, seed=23)
+    off = G.Batch.offsets_of(sets)
+    pts = np.concatenate(sets)
+    n = pts.shape[0]
+    d_pts = torch.from_numpy(pts).cuda()
+    b = G.Batch(lib)
+    stream = torch.cuda.ExternalStream(b.stream())
+    torch.cuda.synchronize()
+    for _ in range(max(3, args.warmup)):
+        if b.execute_device(d_pts.data_ptr(), off) != 0:
+            raise RuntimeError("qdtg_batch_execute_device failed")
+    steps_ms, launches = [], 0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = b.execute_device(d_pts.data_ptr(), off)
+        e1.record(stream)
+        e1.synchronize()
+        if st != 0:
+            raise RuntimeError("qdtg_batch_execute_device failed")
+        steps_ms.append(e0.elapsed_time(e1))
+        launches += b.run_info()["kernel_launches"]
+    ms = statistics.mean(steps_ms)
+    info = b.run_info()
+    # end to end with host buffers
+    e2e_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        if b.execute(pts, off) != 0:
+            raise RuntimeError("qdtg_batch_execute failed")
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e = statistics.mean(e2e_ms)
+    # exactness on a sample of sets (exact checker, outside the timings)
+    viol = None
+    if not args.no_check:
+        viol = 0
+        for i in range(0, len(sets), 64):
+            viol += int(sum(D.check(sets[i], b.triangles(i), b.rep(i)).values()))
+    b.close()
+    del d_pts
+    torch.cuda.empty_cache()
+    # the plain path, once per set
+    t = G.Triangulation(lib)
+    for s in sets[:16]:
+        t.execute(s)
+    t0 = time.perf_counter()
+    for s in sets:
+        if t.execute(s) != 0:
+            raise RuntimeError("qdt_execute failed")
+    plain_s = time.perf_counter() - t0
+    t.close()
+    plain = n / plain_s / 1e6
+    return {
+        "workload": "4096 sets, log-uniform 16..65536 points, square/disk, 10% on a 256 grid (seed 23)",
+        "points": n, "distinct": info["unique_points"], "triangles": info["triangles"],
+        "value": round(n / (ms / 1e3) / 1e6, 3), "ms_per_step": round(ms, 3), "unit": UNIT,
+        "e2e": {"value": round(n / (e2e / 1e3) / 1e6, 3), "ms_per_step": round(e2e, 3),
+                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 24 * info["unique_points"] + 4 * n},
+        "plain_set_by_set": {"value": round(plain, 3), "s": round(plain_s, 3), "unit": UNIT,
+                             "how": "qdt_execute once per set, host buffers"},
+        "speedup_e2e_vs_plain": round((n / (e2e / 1e3) / 1e6) / plain, 2),
+        "gpu_launches": launches, "exact_violations_sampled": viol, "sampled_sets": len(range(0, len(sets), 64)),
+    }
+
+
+def run_serving_leg(lib, args):
+    """Config V: an open-loop Poisson stream of requests (sizes log-uniform in
+    [100, 2,000,000], each uniform, Gaussian-mixture or snapped to a 256
+    grid) at three arrival rates, served by qdtg_server under a 150 GB HBM
+    budget. Latency from scheduled arrival to result in host memory."""
+    from libqdt_gb300 import serving as S
+    from libqdt_gb300 import workloads as W
+
+    base = W.request_stream(args.serve_requests, rate_per_s=1.0, lo=100, hi=2_000_000, seed=29)
+    out = {"workload": "%d requests, log-uniform 100..2e6 points, uniform/gauss/grid (seed 29)" % len(base),
+           "points_per_stream": int(sum(p.shape[0] for _, p in base)), "budget_bytes": 150 << 30, "rates": []}
+    with S.Server(lib) as srv:
+        # warm the engines' pools and the batching path
+        S.run_open_loop(srv, [(0.0, p) for _, p in base[:24]])
+        for rate in (50.0, 200.0, 800.0):
+            reqs = [(at / rate, p) for at, p in base]
+            s0 = srv.stats()
+            r = S.run_open_loop(srv, reqs)
+            s1 = r["stats"]
+            out["rates"].append({"rate_per_s": rate, "p50_ms": round(r["p50_ms"], 3), "p99_ms": round(r["p99_ms"], 3),
+                                 "mpts_per_s": round(r["mpts_per_s"], 3), "completed": r["completed"],
+                                 "coalesced": r["coalesced"], "span_s": round(r["span_s"], 3),
+                                 "rejected": s1["rejected"] - s0["rejected"], "queued": s1["queued"] - s0["queued"],
+                                 "batches": s1["batches"] - s0["batches"]})
+        st = srv.stats()
+        out["rejected"] = st["rejected"]
+        out["queued"] = st["queued"]
+        out["batches"] = st["batches"]
+        out["peak_resident_bytes"] = st["peak_resident_bytes"]
+    return out
 
 
 def main():
@@ -326,6 +448,9 @@ def main():
     ap.add_argument("--workload", default="uniform_2p6m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--legs", default="batched,serving",
+                    help="extra legs in the same line (rank 0, one GPU): batched, serving; '' for none")
+    ap.add_argument("--serve-requests", type=int, default=200)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -47,6 +47,10 @@ QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_t
    on it. */
 QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points);
 
+/* Device bytes of a context's workspace for a batch call on n points (the
+   workspace is kept between calls and grows when a call needs more). */
+QDT_API size_t qdtg_workspace_bytes(size_t n);
+
 /* Fills *info for the last batch call of the context. Returns 1, or 0 when
    ptr or info is NULL. */
 QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info);
@@ -185,6 +189,71 @@ QDT_API void qdtg_batch_set_options(qdtg_batch* b, int count_filter_failures, in
 QDT_API int   qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points);
 QDT_API int   qdtg_batch_get_run_info(const qdtg_batch* b, qdtg_run_info* info);
 QDT_API void* qdtg_batch_stream(const qdtg_batch* b);
+
+/* Pre-allocates the batch's device workspace for up to `points` points in
+   `sets` sets (the workspace otherwise grows on demand), and reports the
+   device bytes it holds. */
+QDT_API qdt_status qdtg_batch_reserve(qdtg_batch* b, size_t points, size_t sets);
+QDT_API size_t     qdtg_batch_workspace_bytes(const qdtg_batch* b);
+
+/* ------------------------------------------------------------------------
+   Serving: a request loop in front of resident GPU engines. No reference
+   counterpart (the reference has only the synchronous per-call API).
+   Requests of at least small_threshold points run on large_workers engines,
+   each with its own CUDA stream and a device workspace kept between
+   requests; smaller requests are coalesced, whenever the batching engine is
+   free, into one many-set call (continuous batching). The device bytes of all
+   workspaces stay within hbm_budget_bytes: a request waits until its
+   engine's workspace fits (idle workspaces are freed to make room); one that
+   cannot fit alone, or that finds max_queue requests waiting, is rejected.
+   Each result is the one qdt_execute() gives for the request alone.
+   ------------------------------------------------------------------------ */
+typedef struct qdtg_server qdtg_server;
+
+typedef struct qdtg_server_config
+{
+    size_t hbm_budget_bytes;   /* default 150 GiB */
+    int    large_workers;      /* engines for large requests, 1..64; default 4 */
+    size_t small_threshold;    /* requests below this many points are coalesced; default 65536 (0: none) */
+    size_t batch_max_points;   /* points per coalesced batch; default 8 Mi */
+    size_t batch_max_sets;     /* requests per coalesced batch; default 4096 */
+    size_t max_queue;          /* waiting requests beyond which new ones are rejected; default 4096 */
+    int    cell_points;        /* as qdtg_set_cell_points; default 0 */
+} qdtg_server_config;
+
+typedef struct qdtg_server_stats
+{
+    unsigned long long submitted, completed, rejected, queued;
+    unsigned long long batches, batched_requests, pool_releases;
+    size_t             resident_bytes, peak_resident_bytes, hbm_budget_bytes;
+    size_t             waiting;     /* requests not yet started */
+} qdtg_server_stats;
+
+QDT_API void qdtg_server_default_config(qdtg_server_config* config);
+/* Starts the worker threads; NULL on bad configuration or no usable GPU. */
+QDT_API qdtg_server* qdtg_server_create(const qdtg_server_config* config);
+/* Finishes every accepted request, then stops the workers and frees all. */
+QDT_API void qdtg_server_destroy(qdtg_server* srv);
+/* Queues a request for n points. The points are read while the request runs:
+   keep them unchanged until it is done. *ticket identifies the request (also
+   a rejected one). Returns QDT_OK when accepted, QDT_ERR_OUT_OF_MEMORY when
+   rejected by the budget or the queue limit, or an argument error (then
+   *ticket is 0). */
+QDT_API qdt_status qdtg_server_submit(qdtg_server* srv, const qdt_vec2d* pts, size_t n, uint64_t* ticket);
+/* Waits until the request is done: 1 done, 0 timed out (timeout_s < 0 waits
+   without limit), -1 unknown ticket. */
+QDT_API int qdtg_server_wait(qdtg_server* srv, uint64_t ticket, double timeout_s);
+/* The request's status (its qdt_execute() status) and results: triangles (3
+   indices each), representatives, distinct count; valid until released. */
+QDT_API qdt_status qdtg_server_result(qdtg_server* srv, uint64_t ticket, const uint32_t** tris, size_t* ntri,
+    const uint32_t** rep, size_t* unique_points);
+/* Milliseconds from submission to start, start to done, submission to done;
+   path 0 = own engine, 1 = coalesced batch. Returns 0 unless done. */
+QDT_API int qdtg_server_timing(qdtg_server* srv, uint64_t ticket, double* queue_ms, double* run_ms,
+    double* total_ms, int* path);
+/* Frees a done request's results; returns 1, or 0 if unknown or not done. */
+QDT_API int  qdtg_server_release(qdtg_server* srv, uint64_t ticket);
+QDT_API void qdtg_server_get_stats(qdtg_server* srv, qdtg_server_stats* stats);
 
 /* Library version string. */
 QDT_API const char* qdtg_version(void);

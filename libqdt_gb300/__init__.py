@@ -30,7 +30,10 @@ GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_get_run_info", 
                "qdtg_batch_set_count", "qdtg_batch_set_status", "qdtg_batch_triangles", "qdtg_batch_unique_points",
                "qdtg_batch_rep", "qdtg_batch_device_triangles", "qdtg_batch_download_device_triangles",
                "qdtg_batch_set_options", "qdtg_batch_set_cell_points", "qdtg_batch_get_run_info",
-               "qdtg_batch_stream")
+               "qdtg_batch_stream", "qdtg_batch_reserve", "qdtg_batch_workspace_bytes", "qdtg_workspace_bytes",
+               "qdtg_server_default_config", "qdtg_server_create", "qdtg_server_destroy", "qdtg_server_submit",
+               "qdtg_server_wait", "qdtg_server_result", "qdtg_server_timing", "qdtg_server_release",
+               "qdtg_server_get_stats")
 
 
 class RunInfo(ctypes.Structure):
@@ -76,6 +79,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_options.restype = None
     lib.qdtg_set_cell_points.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_cell_points.restype = ctypes.c_int
+    lib.qdtg_workspace_bytes.argtypes = [ctypes.c_size_t]
+    lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
     lib.qdtg_get_run_info.argtypes = [P, ctypes.POINTER(RunInfo)]
     lib.qdtg_get_run_info.restype = ctypes.c_int
     lib.qdtg_execute_device.argtypes = [P, P, ctypes.c_size_t, P]
@@ -118,6 +123,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             ("qdtg_batch_download_device_triangles", [P, P, S, P], S),
             ("qdtg_batch_set_options", [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], None),
             ("qdtg_batch_set_cell_points", [P, ctypes.c_int], ctypes.c_int),
+            ("qdtg_batch_reserve", [P, S, S], ctypes.c_int),
+            ("qdtg_batch_workspace_bytes", [P], S),
             ("qdtg_batch_get_run_info", [P, ctypes.POINTER(RunInfo)], ctypes.c_int),
             ("qdtg_batch_stream", [P], P)):
         fn = getattr(lib, name)

@@ -535,6 +535,7 @@ struct BatchEngine
 
     ~BatchEngine()
     {
+        if (!stream && !block && !h_status && !h_words) return;   // never set up (a sizing probe)
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
@@ -614,6 +615,13 @@ size_t bcarve(BatchEngine& g, char* base, size_t N, size_t S)
 }
 
 }  // namespace
+
+// device bytes of a workspace for N points in S sets
+size_t bcarve_bytes(size_t N, size_t S)
+{
+    BatchEngine probe;
+    return bcarve(probe, nullptr, N, S);
+}
 
 int BatchEngine::ensure(size_t N, size_t S)
 {
@@ -1141,6 +1149,24 @@ QDT_API void qdtg_batch_set_options(qdtg_batch* b, int count_filter_failures, in
     b->e.timing = stage_timing != 0;
     b->e.use_graph = use_graphs != 0;
     if (warp_min_points > 0) b->e.warp_min_points = warp_min_points;
+}
+
+QDT_API qdt_status qdtg_batch_reserve(qdtg_batch* b, size_t points, size_t sets)
+{
+    if (!b) return QDT_ERR_NULL_CONTEXT;
+    if (points > qdtg::kMaxPoints) return QDT_ERR_TOO_MANY_POINTS;
+    if (cudaSetDevice(b->e.device) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return QDT_ERR_INTERNAL;
+    }
+    return (qdt_status)b->e.ensure(std::max<size_t>(points, 1), std::max<size_t>(sets, 1));
+}
+
+QDT_API size_t qdtg_batch_workspace_bytes(const qdtg_batch* b)
+{
+    if (!b || !b->e.block) return 0;
+    return qdtg::bcarve_bytes(b->e.capN, b->e.capS);
 }
 
 QDT_API int qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points)

@@ -338,6 +338,8 @@ QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_t
     c->engine->set_timing(stage_timing != 0);
 }
 
+QDT_API size_t qdtg_workspace_bytes(size_t n) { return qdtg::Engine::workspace_bytes(n); }
+
 QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points)
 {
     Context* c = ctx(ptr);

@@ -160,6 +160,33 @@ Engine::~Engine()
     if (stream_) cudaStreamDestroy(stream_);
 }
 
+size_t Engine::workspace_bytes(size_t n)
+{
+    DeviceWork w;
+    return carve(w, nullptr, std::max<size_t>(n, 1024));
+}
+
+size_t Engine::bytes_after(size_t n) const
+{
+    if (w_->block && n <= w_->cap) return w_->bytes;
+    size_t N = std::max<size_t>(n, 1024);
+    if (w_->cap) N = std::max(N, w_->cap + w_->cap / 4);
+    return workspace_bytes(N);
+}
+
+size_t Engine::workspace_bytes() const { return w_->block ? w_->bytes : 0; }
+
+void Engine::release_workspace()
+{
+    if (!w_->block) return;
+    cudaSetDevice(device_);
+    cudaStreamSynchronize(stream_);
+    cudaFree(w_->block);
+    w_->block = nullptr;
+    w_->cap = 0;
+    w_->bytes = 0;
+}
+
 int Engine::ensure(size_t n)
 {
     if (n <= w_->cap && w_->block) return S_OK;

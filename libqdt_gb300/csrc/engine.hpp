@@ -81,6 +81,9 @@ struct RunInfo
 
 struct DeviceWork;
 
+// device bytes of a many-set workspace for N points in S sets (batch.cu)
+size_t bcarve_bytes(size_t N, size_t S);
+
 class Engine
 {
 public:
@@ -99,6 +102,15 @@ public:
     // Triangulates n points already resident on the device. Triangles stay on
     // the device (device_triangles()). Returns a qdt_status value.
     int run_device(const double* d_xy, size_t n, cudaStream_t user_stream);
+
+    // Device bytes of the workspace for n points, and the bytes the
+    // workspace would hold after run_host / run_device on n points (it grows
+    // by at least a quarter when it grows).
+    static size_t workspace_bytes(size_t n);
+    size_t        bytes_after(size_t n) const;
+    size_t        workspace_bytes() const;
+    // frees the workspace (the next call allocates it again)
+    void          release_workspace();
 
     const uint32_t* device_triangles() const;
     const uint32_t* device_rep() const;

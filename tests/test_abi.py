@@ -92,3 +92,28 @@ def test_host_side_checks_without_gpu(lib):
 
 def test_version(lib):
     assert b"sm_103a" in lib.qdtg_version()
+
+
+def test_batch_and_server_host_checks(lib):
+    """Argument checks of the many-set and serving entry points that return
+    before any GPU work, and the workspace sizing used by admission."""
+    from libqdt_gb300 import serving as S
+    S.bind(lib)
+    assert lib.qdtg_batch_execute(None, None, None, 0) == Q.QDT_ERR_NULL_CONTEXT
+    assert lib.qdtg_batch_set_count(None) == 0
+    assert lib.qdtg_batch_triangles(None, 0, None) == 0
+    assert lib.qdtg_batch_set_cell_points(None, 64) == 0
+    w1, w2 = lib.qdtg_workspace_bytes(1_000_000), lib.qdtg_workspace_bytes(2_000_000)
+    assert 250 * 1_000_000 < w1 < 600 * 1_000_000 and w2 > w1
+    c = S.default_config(lib)
+    assert c.hbm_budget_bytes == 150 << 30 and c.large_workers == 4 and c.small_threshold == 65536
+    t = ctypes.c_uint64(5)
+    assert lib.qdtg_server_submit(None, None, 0, ctypes.byref(t)) == Q.QDT_ERR_NULL_CONTEXT
+    bad = S.default_config(lib)
+    bad.large_workers = 0
+    assert not lib.qdtg_server_create(ctypes.byref(bad))
+    bad = S.default_config(lib)
+    bad.small_threshold = bad.batch_max_points + 1
+    assert not lib.qdtg_server_create(ctypes.byref(bad))
+    assert lib.qdtg_server_wait(None, 1, 0.0) == -1
+    assert lib.qdtg_server_release(None, 1) == 0
