@@ -313,7 +313,7 @@ __global__ void k_bfinalize(const uint32_t* __restrict__ A, const uint32_t* __re
 // One depth of every participating set's tree (the single-set k_build_level
 // with the node taken from a list of sets).
 template <bool WARP>
-__global__ void __launch_bounds__(128) k_bbuild_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
+__global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
     NodeOut* __restrict__ nodes, const uint32_t* __restrict__ noff, const uint32_t* __restrict__ list, int nlist,
     const uint32_t* __restrict__ u_off, int d, DevStatus* st, int count)
 {

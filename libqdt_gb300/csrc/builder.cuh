@@ -7,8 +7,13 @@
 #include "common.cuh"
 #include "predicates.cuh"
 
-namespace qdtg {
+// Launch bounds of the level kernels: 128 threads. (A minimum of resident
+// blocks, which would cap the registers, measured no faster: the
+// thread-per-node levels are chains of dependent loads and predicates that
+// run in about one wave.)
+#define QDTG_BUILD_BOUNDS(WARP) __launch_bounds__(128)
 
+namespace qdtg {
 
 __device__ __forceinline__ int sym(int e) { return e ^ 1; }
 

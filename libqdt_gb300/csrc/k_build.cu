@@ -38,7 +38,7 @@ namespace qdtg {
 // their children's results (written by the previous launch). WARP: one node
 // per warp, else one node per thread.
 template <bool WARP>
-__global__ void __launch_bounds__(128) k_build_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
+__global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
     const NodeOut* __restrict__ child, NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count)
 {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
