@@ -439,6 +439,42 @@ def run_serving_leg(lib, args):
     return out
 
 
+def run_profile_target(args):
+    """Runs one form of the path (warmup + steps calls, device-resident input,
+    no timing, no L2 flush, no checks) for a profiler to capture: 'single'
+    (the --workload points) or 'batched' (config B's 4,096 sets)."""
+    import numpy as np
+    import torch
+
+    import libqdt_gb300 as G
+    from libqdt_gb300 import workloads as W
+
+    lib = G.load()
+    if args.profile_run == "single":
+        pts = make_points(args.workload)
+        d = torch.from_numpy(pts).cuda()
+        t = G.Triangulation(lib)
+        for _ in range(args.warmup + args.steps):
+            if t.execute_device(d.data_ptr(), pts.shape[0]) != 0:
+                raise RuntimeError("qdtg_execute_device failed")
+        torch.cuda.synchronize()
+        print("profile run: single %s, %d calls" % (args.workload, args.warmup + args.steps))
+        t.close()
+    else:
+        sets = W.many_sets(count=args.sets, lo=16, hi=65536, seed=23)
+        off = G.Batch.offsets_of(sets)
+        d = torch.from_numpy(np.concatenate(sets)).cuda()
+        b = G.Batch(lib)
+        b.set_options(use_graphs=False)
+        for _ in range(args.warmup + args.steps):
+            if b.execute_device(d.data_ptr(), off) != 0:
+                raise RuntimeError("qdtg_batch_execute_device failed")
+        torch.cuda.synchronize()
+        print("profile run: batched %d sets, %d calls" % (args.sets, args.warmup + args.steps))
+        b.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -451,7 +487,12 @@ def main():
     ap.add_argument("--legs", default="batched,serving",
                     help="extra legs in the same line (rank 0, one GPU): batched, serving; '' for none")
     ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--profile-run", choices=["single", "batched"],
+                    help="only run the path (no timing) for a profiler; see profiles/")
+    ap.add_argument("--sets", type=int, default=4096, help="sets of --profile-run batched")
     args = ap.parse_args()
+    if args.profile_run:
+        return run_profile_target(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -38,6 +38,10 @@ namespace qdtg {
 
 namespace {
 
+// words per set for the per-height entry lists: at most 2 entries per set and
+// height, heights < 28 (sets of at most 1e8 points), plus one offset per height
+constexpr size_t kEntWords = 64;
+
 constexpr int kBThreads = 256;
 constexpr int kBRounds = 8;
 constexpr int kBTile = kBThreads * kBRounds;
@@ -310,34 +314,47 @@ __global__ void k_bfinalize(const uint32_t* __restrict__ A, const uint32_t* __re
     vid[i] = uid[u];
 }
 
-// One depth of every participating set's tree (the single-set k_build_level
-// with the node taken from a list of sets).
-template <bool WARP>
-__global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
-    NodeOut* __restrict__ nodes, const uint32_t* __restrict__ noff, const uint32_t* __restrict__ list, int nlist,
-    const uint32_t* __restrict__ u_off, int d, DevStatus* st, int count)
+// All nodes of one height (the levels below them) in every participating
+// set. Nodes of equal height have sizes within a factor of two, so the
+// merges of a launch are alike, whatever the sizes of their sets; a node's
+// children have smaller heights and were built by earlier launches. A node
+// of height h lies at depth D - h (D the set's split depth) or, when it is a
+// smaller sibling, at D - h - 1: the launch runs over entries (set, depth)
+// with 2^depth slots each (entry e covers slots [eoff[e], eoff[e + 1])) and
+// skips the slots whose node has another height. The single-set
+// k_build_level is the same body with depth-synchronous launches (there all
+// nodes of a depth are alike).
+template <bool WARP, bool LEAF>
+__global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_height(Rec* __restrict__ R, int nrec,
+    const double2* __restrict__ V, NodeOut* __restrict__ nodes, const uint32_t* __restrict__ noff,
+    const uint32_t* __restrict__ ent, const uint32_t* __restrict__ eoff, int nent, const uint32_t* __restrict__ u_off,
+    int h, DevStatus* st, int count)
 {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long flat = WARP ? (g >> 5) : g;
     const int       lane = WARP ? (int)(threadIdx.x & 31) : 0;
-    if (flat >= ((long long)nlist << d)) return;
+    if (flat >= (long long)eoff[nent]) return;
     unsigned flags = *(volatile unsigned*)&st->flags;
     if (WARP) flags = __shfl_sync(0xffffffffu, flags, 0);
     if (flags & kFatal) return;
-    const uint32_t  s = list[flat >> d];
-    const long long k = flat & ((1ll << d) - 1);
+    const uint32_t  e = find_set(eoff, nent, (uint32_t)flat);
+    const uint32_t  s = ent[e] >> 5;
+    const int       d = (int)(ent[e] & 31u);
+    const long long k = flat - eoff[e];
     const int       base = (int)u_off[s], ms = (int)(u_off[s + 1] - u_off[s]);
     int             lo, hi;
-    if (!node_range(ms, d, k, lo, hi)) return;
+    if (!node_range(ms, d, k, lo, hi) || subtree_levels(hi - lo) != h) return;
     lo += base;
     hi += base;
     NodeOut* const out = nodes + noff[s];   // heap order: (1 << depth) + index
     Builder        B{ R, nrec, st, count ? &st->pc : nullptr, -1, -1, false };
     const int      n = hi - lo;
     NodeOut        o;
-    if (n <= 3)
+    // height 0 is all leaves, the other heights all merges: two kernels, so
+    // that neither carries the other's code
+    if (LEAF || n <= 3)
     {
-        if (lane != 0) return;
+        if (!LEAF || lane != 0) return;
         B.leaf(lo, hi, V, o.le, o.re);
     }
     else
@@ -502,7 +519,8 @@ struct BatchEngine
     uint32_t* vid = nullptr;
     Rec*      recs = nullptr;
     NodeOut*  nodes = nullptr;
-    uint32_t *noff = nullptr, *lists = nullptr, *tri_off = nullptr, *tris = nullptr, *tri_base = nullptr;
+    uint32_t *noff = nullptr, *ents = nullptr, *eoffs = nullptr, *tri_off = nullptr, *tris = nullptr,
+             *tri_base = nullptr;
     uint32_t* cell_off = nullptr;
     uint32_t *counts = nullptr, *offs = nullptr, *scratch = nullptr, *words = nullptr;
     DevStatus* status = nullptr;
@@ -510,8 +528,9 @@ struct BatchEngine
     // host results (pinned)
     PinnedVec<uint32_t> h_tris, h_rep, h_tri_base, h_u_off, h_in_off;
     PinnedVec<uint8_t>  h_bad;
-    std::vector<uint32_t> h_noff, h_lists;
-    std::vector<int>      h_list_off;
+    std::vector<uint32_t> h_noff, h_ents, h_eoffs;
+    // per height: first entry, number of entries, first offset word
+    std::vector<int>      h_ent0, h_nent, h_eoff0;
     DevStatus*            h_status = nullptr;
     uint32_t*             h_words = nullptr;
     size_t                nsets = 0, npts = 0, ntri = 0;
@@ -522,7 +541,6 @@ struct BatchEngine
     int                   cell_points = 0;         // largest cell built in shared memory (0: none)
     std::vector<uint32_t> h_cell_off;
     uint32_t              ncells = 0;
-    int                   Dglob = -1;   // deepest depth of the level launches
     cudaEvent_t           ev[8] = {};
     // CUDA graphs of the post-synchronisation part, by batch shape
     struct GraphEntry
@@ -549,6 +567,9 @@ struct BatchEngine
 
     int ensure(size_t N, size_t S);
     int run(size_t N, size_t S, bool host_io);
+    // nodes of height h have more than 3 * 2^(h-1) points: a warp per node when
+    // that reaches warp_min_points
+    bool height_warp(int h) const { return h >= 1 && 3ll * (1ll << (h - 1)) + 1 >= warp_min_points; }
     void post_sync_work(size_t N, size_t S, uint32_t M, int Dmax);
 };
 
@@ -602,7 +623,8 @@ size_t bcarve(BatchEngine& g, char* base, size_t N, size_t S)
     g.tri_base = c.take<uint32_t>(S + 1);
     g.noff = c.take<uint32_t>(S + 1);
     g.cell_off = c.take<uint32_t>(S + 1);
-    g.lists = c.take<uint32_t>(40 * (S + 1));
+    g.ents = c.take<uint32_t>(kEntWords * (S + 1));
+    g.eoffs = c.take<uint32_t>(kEntWords * (S + 1));
     g.counts = c.take<uint32_t>(tiles);
     g.offs = c.take<uint32_t>(tiles);
     g.scratch = c.take<uint32_t>(std::max(scan_scratch_words(3 * N), scan_scratch_words(tiles)));
@@ -713,25 +735,27 @@ void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax)
             nodes, noff, cell_off, (int)S, u_off, cell_points, ncells, status, count_filter ? 1 : 0);
         ++launch_counter();
     }
-    // the levels above: per depth, one launch over the large nodes (a warp
-    // each) and one over the small ones (a thread each) of every set that has
-    // the depth
-    for (int d = Dglob; d >= 0; --d)
+    // the nodes above: one launch per height, from the leaves up; a warp per
+    // node for the heights whose nodes have at least warp_min_points points
+    for (int h = 0; h < (int)h_nent.size(); ++h)
     {
-        for (int mode = 0; mode < 2; ++mode)
-        {
-            const int nl = h_list_off[2 * d + mode + 1] - h_list_off[2 * d + mode];
-            if (nl == 0) continue;
-            const long long nodes_d = (long long)nl << d;
-            const uint32_t* lst = lists + h_list_off[2 * d + mode];
-            if (mode == 0)
-                k_bbuild_level<true><<<(unsigned)((nodes_d * 32 + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes,
-                    noff, lst, nl, u_off, d, status, count_filter ? 1 : 0);
-            else
-                k_bbuild_level<false><<<(unsigned)((nodes_d + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes, noff,
-                    lst, nl, u_off, d, status, count_filter ? 1 : 0);
-            ++launch_counter();
-        }
+        const int nent = h_nent[h];
+        if (nent == 0) continue;
+        const long long slots = h_eoffs[h_eoff0[h] + nent];
+        if (slots == 0) continue;
+        const uint32_t* en = ents + h_ent0[h];
+        const uint32_t* eo = eoffs + h_eoff0[h];
+        const int cf = count_filter ? 1 : 0;
+        if (h == 0)
+            k_bbuild_height<false, true><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes, noff,
+                en, eo, nent, u_off, h, status, cf);
+        else if (height_warp(h))
+            k_bbuild_height<true, false><<<(unsigned)((slots * 32 + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes,
+                noff, en, eo, nent, u_off, h, status, cf);
+        else
+            k_bbuild_height<false, false><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes, noff,
+                en, eo, nent, u_off, h, status, cf);
+        ++launch_counter();
     }
     if (timing) cudaEventRecord(ev[5], s);
     k_btri_mask<<<gridn(nrec, 256), 256, 0, s>>>(recs, nrec, useg, skip, mask, status, count_filter ? 1 : 0);
@@ -799,15 +823,14 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
     }
     const uint32_t M = h_u_off[S];
     info.unique_points = M;
-    // plan the trees: depth lists and node heaps
+    // plan the trees: node heaps, cells, per-height entry lists
     // Each set of m distinct points splits down to depth split_levels(m); the
-    // cells cover the depths from cell_depth(m, C) down, the level launches
-    // the depths above (all depths without cells).
+    // cells cover the depths from cell_depth(m, C) down, the height launches
+    // the nodes above (all nodes without cells).
     const int            C = cell_points;
     std::vector<uint8_t> skipv(S);
-    std::vector<int>     top(S, -1);   // deepest depth built by the level launches
+    std::vector<int>     top(S, -1);   // deepest depth built by the height launches
     int                  Dmax = 0;     // deepest split
-    Dglob = -1;
     h_noff.assign(S + 1, 0);
     h_cell_off.assign(S + 1, 0);
     size_t nacc = 0, cacc = 0;
@@ -830,34 +853,50 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
             }
             else
                 top[i] = Ds;
-            Dglob = std::max(Dglob, top[i]);
         }
     }
     h_noff[S] = (uint32_t)nacc;
     h_cell_off[S] = (uint32_t)cacc;
     ncells = (uint32_t)cacc;
     if (nacc > nodes_cap || cacc > 0xFFFFFFFFull) return QDT_ERR_INTERNAL;
-    // per depth two lists: the sets whose nodes at that depth are large enough
-    // for one warp per node, then the others (one thread per node)
-    h_list_off.assign(2 * (Dglob + 1) + 1, 0);
-    h_lists.clear();
-    for (int d = 0; d <= Dglob; ++d)
-        for (int mode = 0; mode < 2; ++mode)
+    // per height the entries (set, depth) that hold nodes of that height (at
+    // depths D - h and D - h - 1, above the cells), with their slot offsets
+    int Hmax = -1;
+    for (size_t i = 0; i < S; ++i)
+        if (!skipv[i]) Hmax = std::max(Hmax, split_levels((int)(h_u_off[i + 1] - h_u_off[i])));
+    h_ent0.assign(Hmax + 1, 0);
+    h_nent.assign(Hmax + 1, 0);
+    h_eoff0.assign(Hmax + 1, 0);
+    h_ents.clear();
+    h_eoffs.clear();
+    for (int h = 0; h <= Hmax; ++h)
+    {
+        h_ent0[h] = (int)h_ents.size();
+        h_eoff0[h] = (int)h_eoffs.size();
+        uint64_t acc = 0;
+        for (size_t i = 0; i < S; ++i)
         {
-            h_list_off[2 * d + mode] = (int)h_lists.size();
-            for (size_t i = 0; i < S; ++i)
+            if (skipv[i]) continue;
+            const int Ds = split_levels((int)(h_u_off[i + 1] - h_u_off[i]));
+            for (int d = Ds - h; d >= Ds - h - 1; --d)
             {
-                if (skipv[i] || top[i] < d) continue;
-                const bool warp = ((h_u_off[i + 1] - h_u_off[i]) >> d) >= (uint32_t)warp_min_points;
-                if (warp == (mode == 0)) h_lists.push_back((uint32_t)i);
+                if (d < 0 || d > top[i]) continue;
+                h_ents.push_back(((uint32_t)i << 5) | (uint32_t)d);
+                h_eoffs.push_back((uint32_t)acc);
+                acc += (uint64_t)1 << d;
             }
         }
-    h_list_off[2 * (Dglob + 1)] = (int)h_lists.size();
-    if (h_lists.size() > 40 * (capS + 1)) return QDT_ERR_INTERNAL;
+        if (acc > 0xFFFFFFFFull) return QDT_ERR_INTERNAL;
+        h_nent[h] = (int)h_ents.size() - h_ent0[h];
+        h_eoffs.push_back((uint32_t)acc);
+    }
+    if (h_ents.size() > kEntWords * (capS + 1) || h_eoffs.size() > kEntWords * (capS + 1) || S >= (1u << 27))
+        return QDT_ERR_INTERNAL;
     cudaMemcpyAsync(skip, skipv.data(), S, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(noff, h_noff.data(), (S + 1) * 4, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(cell_off, h_cell_off.data(), (S + 1) * 4, cudaMemcpyHostToDevice, s);
-    if (!h_lists.empty()) cudaMemcpyAsync(lists, h_lists.data(), h_lists.size() * 4, cudaMemcpyHostToDevice, s);
+    if (!h_ents.empty()) cudaMemcpyAsync(ents, h_ents.data(), h_ents.size() * 4, cudaMemcpyHostToDevice, s);
+    if (!h_eoffs.empty()) cudaMemcpyAsync(eoffs, h_eoffs.data(), h_eoffs.size() * 4, cudaMemcpyHostToDevice, s);
     if (C > 0)
         cudaFuncSetAttribute(k_bbuild_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
             cell_block_warps(C) * cell_smem_bytes(C));

@@ -80,6 +80,13 @@ struct GlobalMap
         e = chk(e);
         return R[e >> 1].p[e & 1];
     }
+    // onext (dir 0) or oprev (dir 1) with one load: next[2] and prev[2] are
+    // adjacent in the record
+    __device__ __forceinline__ int ring(int e, int dir)
+    {
+        e = chk(e);
+        return (&R[e >> 1].next[0])[2 * dir + (e & 1)];
+    }
 
     // the ids written here were all read through onext/oprev just before,
     // which checked them
@@ -199,6 +206,11 @@ struct CellMap
     {
         // a dead record's origin is -1: the clamp keeps the read in the cell
         return V[min((unsigned)org(e), (unsigned)(nv - 1))];
+    }
+    __device__ __forceinline__ int ring(int e, int dir)
+    {
+        e = chk(e);
+        return (&R[e >> 1].next[0])[2 * dir + (e & 1)];
     }
     __device__ __forceinline__ void set_next(int e, int v)
     {
@@ -387,6 +399,49 @@ struct MapBuilder : Map
         return basel;
     }
 
+    // The same walk with one orient2d call site for both tests: shorter code
+    // for the warp merge, whose first lane walks the tangent alone (measured
+    // faster there, slower in the thread-per-node merges, which prefer the
+    // form above with one load fewer per test).
+    __device__ int tangent_one_site(int& ldo, int& ldi, int& rdi, int& rdo, int lim)
+    {
+        // leftOf(org(rdi), ldi) = ccw(org(rdi), org(ldi), dest(ldi)); when it
+        // fails, rightOf(org(ldi), rdi) = ccw(org(ldi), dest(rdi), org(rdi))
+        // (second: the rightOf test is next)
+        int  it = 0;
+        bool second = false;
+        for (;;)
+        {
+            if (bad) return 0;
+            if (++it > 2 * lim)
+            {
+                fail(ST_GUARD);
+                return 0;
+            }
+            const double2 prdi = porg(rdi), pldi = porg(ldi);
+            const double2 b = porg(second ? sym(rdi) : ldi);
+            const double2 c = porg(second ? rdi : sym(ldi));
+            if (ccw(second ? pldi : prdi, b, c, pc))
+            {
+                if (second)
+                {
+                    rdi = rprev(rdi);
+                    second = false;
+                }
+                else
+                    ldi = lnext(ldi);
+            }
+            else if (second)
+                break;
+            else
+                second = true;
+        }
+        const int basel = connect(sym(rdi), ldi);
+        if (org(ldi) == org(ldo)) ldo = sym(basel);
+        if (org(rdi) == org(rdo)) rdo = basel;
+        return basel;
+    }
+
     // reference builder.hxx:251-285 (with the scans :205-249 in line)
     __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
     {
@@ -402,61 +457,52 @@ struct MapBuilder : Map
             }
             const int     bo = org(basel), bd = dest(basel);
             const double2 pbo = porg(basel), pbd = pdest(basel);
-            // left candidate (builder.hxx:205-226)
-            int     lc = onext(sym(basel));
-            int     lcd = dest(lc);
-            double2 plcd = pdest(lc);
-            bool    lv = ccw(plcd, pbd, pbo, pc);
-            if (lv)
+            int           lc = 0, lcd = 0, rc = 0, rcd = 0;
+            double2       plcd = pbo, prcd = pbo;
+            bool          lv = false, rv = false;
+            // the two candidate scans, left then right, as one loop over the
+            // sides so that their predicate calls share code: side 0 walks
+            // the ring of bd counter-clockwise from onext(sym(basel))
+            // (builder.hxx:205-226), side 1 the ring of bo clockwise from
+            // oprev(basel) (:228-249)
+#pragma unroll 1
+            for (int side = 0; side < 2; ++side)
             {
-                bool deleted = false;
-                int  j = 0;
-                for (;;)
+                int     c = side ? oprev(basel) : onext(sym(basel));
+                int     cd = dest(c);
+                double2 pcd = pdest(c);
+                bool    v = false;
+                // validE(c); if valid, the delete loop, and validE again after
+                // deletions (one call site for both validity tests)
+                for (int pass = 0;; ++pass)
                 {
-                    const int     t = onext(lc);
-                    const int     td = dest(t);
-                    const double2 ptd = pdest(t);
-                    if (!in_circle(bd, pbd, bo, pbo, lcd, plcd, td, ptd)) break;
-                    if (bad || ++j > lim)
+                    v = ccw(pcd, pbd, pbo, pc);
+                    if (!v || pass) break;
+                    bool deleted = false;
+                    int  j = 0;
+                    for (;;)
                     {
-                        fail(ST_GUARD);
-                        return;
+                        const int     t = this->ring(c, side);
+                        const int     td = dest(t);
+                        const double2 ptd = pdest(t);
+                        if (!in_circle(bd, pbd, bo, pbo, cd, pcd, td, ptd)) break;
+                        if (bad || ++j > lim)
+                        {
+                            fail(ST_GUARD);
+                            return;
+                        }
+                        delete_edge(c);
+                        c = t;
+                        cd = td;
+                        pcd = ptd;
+                        deleted = true;
                     }
-                    delete_edge(lc);
-                    lc = t;
-                    lcd = td;
-                    plcd = ptd;
-                    deleted = true;
+                    if (!deleted) break;
                 }
-                if (deleted) lv = ccw(plcd, pbd, pbo, pc);
-            }
-            // right candidate (builder.hxx:228-249)
-            int     rc = oprev(basel);
-            int     rcd = dest(rc);
-            double2 prcd = pdest(rc);
-            bool    rv = ccw(prcd, pbd, pbo, pc);
-            if (rv)
-            {
-                bool deleted = false;
-                int  j = 0;
-                for (;;)
-                {
-                    const int     t = oprev(rc);
-                    const int     td = dest(t);
-                    const double2 ptd = pdest(t);
-                    if (!in_circle(bd, pbd, bo, pbo, rcd, prcd, td, ptd)) break;
-                    if (bad || ++j > lim)
-                    {
-                        fail(ST_GUARD);
-                        return;
-                    }
-                    delete_edge(rc);
-                    rc = t;
-                    rcd = td;
-                    prcd = ptd;
-                    deleted = true;
-                }
-                if (deleted) rv = ccw(prcd, pbd, pbo, pc);
+                if (side)
+                    rc = c, rcd = cd, prcd = pcd, rv = v;
+                else
+                    lc = c, lcd = cd, plcd = pcd, lv = v;
             }
             if (!lv && !rv) break;
             if (!lv || (rv && in_circle(lcd, plcd, bd, pbd, bo, pbo, rcd, prcd)))
@@ -586,7 +632,7 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
     const int      jj = slot ? j : 0;               // window slot this lane keeps
 
     int basel = 0;
-    if (lane == 0) basel = B.tangent(ldo, ldi, rdi, rdo, lim);
+    if (lane == 0) basel = B.tangent_one_site(ldo, ldi, rdi, rdo, lim);
     __syncwarp();
     basel = __shfl_sync(FULL, basel, 0);
     bool bad = __shfl_sync(FULL, (int)B.bad, 0) != 0;

@@ -525,13 +525,13 @@ QDT_HD __forceinline__ int incircle_f32(double adx_, double ady_, double bdx_, d
 // Filtered predicates (reference robust.hxx:337-347, :377-396)
 // ---------------------------------------------------------------------------
 
-QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double by, double cx, double cy,
-    PredCounters* ctr = nullptr)
+// The double filter and the exact evaluation run only when the single-
+// precision filter cannot decide: they are out of line (one copy each), so
+// that the code of a merge loop, which calls the predicates from many
+// places, stays small enough for the instruction cache.
+static QDT_HD __noinline__ int orient2d_slow(double ax, double ay, double bx, double by, double cx, double cy,
+    PredCounters* ctr)
 {
-    {
-        const int s = orient2d_f32(sub_rn(ax, cx), sub_rn(ay, cy), sub_rn(bx, cx), sub_rn(by, cy));
-        if (s) return s;
-    }
     const double detleft = mul_rn(sub_rn(ax, cx), sub_rn(by, cy));
     const double detright = mul_rn(sub_rn(ay, cy), sub_rn(bx, cx));
     const double det = sub_rn(detleft, detright);
@@ -547,16 +547,12 @@ QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double
     return orient2d_exact(v);
 }
 
-QDT_HD __forceinline__ int incircle_sign(double ax, double ay, double bx, double by, double cx, double cy,
-    double dx, double dy, PredCounters* ctr = nullptr)
+static QDT_HD __noinline__ int incircle_slow(double ax, double ay, double bx, double by, double cx, double cy,
+    double dx, double dy, PredCounters* ctr)
 {
     const double adx = sub_rn(ax, dx), ady = sub_rn(ay, dy);
     const double bdx = sub_rn(bx, dx), bdy = sub_rn(by, dy);
     const double cdx = sub_rn(cx, dx), cdy = sub_rn(cy, dy);
-    {
-        const int s = incircle_f32(adx, ady, bdx, bdy, cdx, cdy);
-        if (s) return s;
-    }
     const double bdxcdy = mul_rn(bdx, cdy), cdxbdy = mul_rn(cdx, bdy);
     const double cdxady = mul_rn(cdx, ady), adxcdy = mul_rn(adx, cdy);
     const double adxbdy = mul_rn(adx, bdy), bdxady = mul_rn(bdx, ady);
@@ -578,6 +574,21 @@ QDT_HD __forceinline__ int incircle_sign(double ax, double ay, double bx, double
 #endif
     const double v[8] = { ax, ay, bx, by, cx, cy, dx, dy };
     return incircle_exact(v);
+}
+
+QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double by, double cx, double cy,
+    PredCounters* ctr = nullptr)
+{
+    const int s = orient2d_f32(sub_rn(ax, cx), sub_rn(ay, cy), sub_rn(bx, cx), sub_rn(by, cy));
+    return s ? s : orient2d_slow(ax, ay, bx, by, cx, cy, ctr);
+}
+
+QDT_HD __forceinline__ int incircle_sign(double ax, double ay, double bx, double by, double cx, double cy,
+    double dx, double dy, PredCounters* ctr = nullptr)
+{
+    const int s = incircle_f32(sub_rn(ax, dx), sub_rn(ay, dy), sub_rn(bx, dx), sub_rn(by, dy), sub_rn(cx, dx),
+        sub_rn(cy, dy));
+    return s ? s : incircle_slow(ax, ay, bx, by, cx, cy, dx, dy, ctr);
 }
 
 }  // namespace qdtg
