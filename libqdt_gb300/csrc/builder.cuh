@@ -476,7 +476,8 @@ struct MapBuilder : Map
                 // deletions (one call site for both validity tests)
                 for (int pass = 0;; ++pass)
                 {
-                    v = ccw(pcd, pbd, pbo, pc);
+                    // a candidate ending at bo or bd is collinear: not valid
+                    v = cd != bo && cd != bd && ccw(pcd, pbd, pbo, pc);
                     if (!v || pass) break;
                     bool deleted = false;
                     int  j = 0;
@@ -685,7 +686,10 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
             const int     src_a = combo ? ca : 0, src_b = combo ? 16 + rb : 16;
             const int     ad = __shfl_sync(FULL, mine.d, src_a), bdst = __shfl_sync(FULL, mine.d, src_b);
             const double2 pa = shfl_d2(mine.p, src_a), pb = shfl_d2(mine.p, src_b);
-            const bool valid = slot && ccw(mine.p, pbd, pbo, B.pc);
+            // a candidate that ends at bo or bd (a window that wrapped around a
+            // short ring) is collinear with the base edge: not valid, decided by
+            // its id without a predicate (distinct ids have distinct points)
+            const bool valid = slot && mine.d != bo && mine.d != bd && ccw(mine.p, pbd, pbo, B.pc);
             // one in-circle call for both roles, so the lanes share one
             // instruction stream: slot (bd, bo, dest c_j, dest c_j+1),
             // choice (dest c_a, bd, bo, dest r_b)
