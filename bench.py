@@ -197,6 +197,10 @@ def run_gb300(args):
     pts = make_points(args.workload)
     n = pts.shape[0]
     lib = G.load()
+    # the schedule knobs for this GPU: cached, or measured now (outside every
+    # timed region; they change the speed, not the results)
+    from libqdt_gb300 import autotune
+    tuning = autotune.ensure(lib) if not args.no_tune else None
     t = G.Triangulation(lib)
     t.set_options(count_filter_failures=False, stage_timing=True)
     d_pts = torch.from_numpy(pts).cuda().contiguous()
@@ -287,7 +291,10 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform [0,1)^2)",
         "config": {"workload": args.workload, "points": n, "distinct": m, "triangles": ntri,
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "single"},
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "single",
+                   "tuning": ({k: tuning[k] for k in ("cell_points", "single_warp_min_points",
+                                                      "batch_warp_min_points", "server_large_workers")}
+                              if tuning else "defaults")},
         "exact_violations": viol,
         "stage_ms": {k[3:]: round(v, 4) for k, v in stage_ms.items()},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -487,6 +494,7 @@ def main():
     ap.add_argument("--legs", default="batched,serving",
                     help="extra legs in the same line (rank 0, one GPU): batched, serving; '' for none")
     ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner's choice")
     ap.add_argument("--profile-run", choices=["single", "batched"],
                     help="only run the path (no timing) for a profiler; see profiles/")
     ap.add_argument("--sets", type=int, default=4096, help="sets of --profile-run batched")

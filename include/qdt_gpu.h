@@ -51,6 +51,28 @@ QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points);
    workspace is kept between calls and grows when a call needs more). */
 QDT_API size_t qdtg_workspace_bytes(size_t n);
 
+/* The name of the current CUDA device into out (cap bytes, terminated);
+   returns 0 (and an empty string) when no device is usable. */
+QDT_API int qdtg_device_name(char* out, size_t cap);
+
+/* The smallest node (points) that the context's build merges with a whole
+   warp instead of one thread (default 512). Returns 1, or 0 for a NULL
+   context, a value below 1 or no usable GPU. The triangulation does not
+   depend on it. */
+QDT_API int qdtg_set_warp_min_points(qdt_t* ptr, int warp_min_points);
+
+/* Process-wide defaults of the schedule knobs, taken by every context, batch
+   and server created afterwards (the autotuner of the Python package sets
+   them from its per-GPU cache): shared-memory cell size (0: none), the warp
+   thresholds of the single-set and many-set builds, and the serving
+   engines. A negative value (0 for the last three) keeps the current one.
+   Returns 0 and changes nothing for a value out of range. Call before
+   creating contexts; not synchronised with concurrent creation. */
+QDT_API int  qdtg_set_defaults(int cell_points, int single_warp_min_points, int batch_warp_min_points,
+    int server_large_workers);
+QDT_API void qdtg_get_defaults(int* cell_points, int* single_warp_min_points, int* batch_warp_min_points,
+    int* server_large_workers);
+
 /* Fills *info for the last batch call of the context. Returns 1, or 0 when
    ptr or info is NULL. */
 QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info);

@@ -22,7 +22,8 @@ from .qdt_api import (QDT_OK, QDT_ERR_NULL_CONTEXT, QDT_ERR_NULL_ARGUMENT, QDT_E
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
-GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
+GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_min_points", "qdtg_set_defaults",
+               "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
                "qdtg_incircle", "qdtg_eval_predicates", "qdtg_unique_points_noalloc", "qdtg_version",
@@ -81,6 +82,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_cell_points.restype = ctypes.c_int
     lib.qdtg_workspace_bytes.argtypes = [ctypes.c_size_t]
     lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
+    lib.qdtg_set_warp_min_points.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_warp_min_points.restype = ctypes.c_int
+    lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 4
+    lib.qdtg_set_defaults.restype = ctypes.c_int
+    lib.qdtg_device_name.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.qdtg_device_name.restype = ctypes.c_int
+    lib.qdtg_get_defaults.argtypes = [ctypes.POINTER(ctypes.c_int)] * 4
+    lib.qdtg_get_defaults.restype = None
     lib.qdtg_get_run_info.argtypes = [P, ctypes.POINTER(RunInfo)]
     lib.qdtg_get_run_info.restype = ctypes.c_int
     lib.qdtg_execute_device.argtypes = [P, P, ctypes.c_size_t, P]
@@ -131,6 +140,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         fn.argtypes = args
         fn.restype = res
     _lib = lib
+    # the autotuner's choice for this GPU, when one is cached (it changes the
+    # schedule, not the results)
+    from . import autotune
+    autotune.load_cached(lib)
     return lib
 
 
@@ -173,6 +186,9 @@ class Triangulation(qdt_api.Context):
 
     def set_cell_points(self, cell_points: int) -> bool:
         return self.lib.qdtg_set_cell_points(self.ptr, int(cell_points)) == 1
+
+    def set_warp_min_points(self, points: int) -> bool:
+        return self.lib.qdtg_set_warp_min_points(self.ptr, int(points)) == 1
 
     def execute_device(self, d_ptr: int, n: int, stream: int = 0) -> int:
         return self.lib.qdtg_execute_device(self.ptr, d_ptr, n, stream or None)

@@ -527,6 +527,7 @@ struct BatchEngine
     size_t     nodes_cap = 0;
     // host results (pinned)
     PinnedVec<uint32_t> h_tris, h_rep, h_tri_base, h_u_off, h_in_off;
+    PinnedVec<double>   h_pts;   // staging of host input
     PinnedVec<uint8_t>  h_bad;
     std::vector<uint32_t> h_noff, h_ents, h_eoffs;
     // per height: first entry, number of entries, first offset word
@@ -1061,9 +1062,28 @@ qdt_status batch_run(qdtg_batch* b, const qdt_vec2d* pts, bool device_in, const 
             cudaStreamWaitEvent(e.stream, e.ev[7], 0);
         }
         cudaMemcpyAsync(e.in_off, e.h_in_off.data(), (nsets + 1) * 4, cudaMemcpyHostToDevice, e.stream);
-        if (N)
+        cudaPointerAttributes attr{};
+        const bool pinned = !device_in && N && cudaPointerGetAttributes(&attr, pts) == cudaSuccess &&
+                            attr.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (N && (device_in || pinned))
             cudaMemcpyAsync(e.pts, pts, N * sizeof(double2), device_in ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                 e.stream);
+        else if (N)
+        {
+            // through page-locked staging in chunks: the host copy of a chunk
+            // overlaps the upload of the previous one
+            e.h_pts.resize(2 * N);
+            const size_t chunk = (size_t)1 << 18;
+            const double* src = reinterpret_cast<const double*>(pts);
+            for (size_t o = 0; o < N; o += chunk)
+            {
+                const size_t c = std::min(chunk, N - o);
+                std::memcpy(e.h_pts.data() + 2 * o, src + 2 * o, c * sizeof(double2));
+                cudaMemcpyAsync(e.pts + o, e.h_pts.data() + 2 * o, c * sizeof(double2), cudaMemcpyHostToDevice,
+                    e.stream);
+            }
+        }
         e.npts = N;
         e.nsets = nsets;
         const int r = e.run(N, nsets, !device_in);
@@ -1106,6 +1126,8 @@ QDT_API qdtg_batch* qdtg_batch_create(void)
         return nullptr;
     }
     for (auto& ev : e.ev) cudaEventCreate(&ev);
+    e.cell_points = qdtg::tuning().cell_points;
+    e.warp_min_points = qdtg::tuning().batch_warp_min_points;
     return b;
 }
 

@@ -2,7 +2,10 @@
 // codes, reset-on-failure, queries. Mirrors the reference shim
 // (libqdt/qdt.cpp) function by function; no C++ exception crosses it.
 #include <cmath>
+#include <cstring>
 #include <new>
+
+#include <cuda_runtime.h>
 
 #include "common.cuh"
 #include "context.hpp"
@@ -339,6 +342,54 @@ QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_t
 }
 
 QDT_API size_t qdtg_workspace_bytes(size_t n) { return qdtg::Engine::workspace_bytes(n); }
+
+QDT_API int qdtg_device_name(char* out, size_t cap)
+{
+    if (!out || cap == 0) return 0;
+    out[0] = 0;
+    int dev = 0, count = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0 || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 0;
+    }
+    std::strncpy(out, prop.name, cap - 1);
+    out[cap - 1] = 0;
+    return 1;
+}
+
+QDT_API int qdtg_set_defaults(int cell_points, int single_warp_min_points, int batch_warp_min_points,
+    int server_large_workers)
+{
+    if (cell_points > qdtg::kCellMax || (cell_points > 0 && cell_points < 4) || server_large_workers > 64) return 0;
+    qdtg::Tuning& t = qdtg::tuning();
+    if (cell_points >= 0) t.cell_points = cell_points;
+    if (single_warp_min_points > 0) t.single_warp_min_points = single_warp_min_points;
+    if (batch_warp_min_points > 0) t.batch_warp_min_points = batch_warp_min_points;
+    if (server_large_workers > 0) t.server_large_workers = server_large_workers;
+    return 1;
+}
+
+QDT_API void qdtg_get_defaults(int* cell_points, int* single_warp_min_points, int* batch_warp_min_points,
+    int* server_large_workers)
+{
+    const qdtg::Tuning& t = qdtg::tuning();
+    if (cell_points) *cell_points = t.cell_points;
+    if (single_warp_min_points) *single_warp_min_points = t.single_warp_min_points;
+    if (batch_warp_min_points) *batch_warp_min_points = t.batch_warp_min_points;
+    if (server_large_workers) *server_large_workers = t.server_large_workers;
+}
+
+QDT_API int qdtg_set_warp_min_points(qdt_t* ptr, int warp_min_points)
+{
+    Context* c = ctx(ptr);
+    if (!c || warp_min_points < 1) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_warp_min_points(warp_min_points);
+    return 1;
+}
 
 QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points)
 {

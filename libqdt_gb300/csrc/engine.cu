@@ -122,6 +122,8 @@ Engine* Engine::create(int* cuda_error)
     Engine* g = new (std::nothrow) Engine();
     if (!g) return nullptr;
     g->device_ = dev;
+    g->cell_points_ = tuning().cell_points;
+    g->warp_min_points_ = tuning().single_warp_min_points;
     if (cudaStreamCreateWithFlags(&g->stream_, cudaStreamNonBlocking) != cudaSuccess)
     {
         cudaGetLastError();
@@ -158,6 +160,12 @@ Engine::~Engine()
     for (auto& ev : ev_)
         if (ev) cudaEventDestroy(ev);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+Tuning& tuning()
+{
+    static Tuning t;
+    return t;
 }
 
 size_t Engine::workspace_bytes(size_t n)
@@ -250,6 +258,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     info_.unique_points = m;
     b.count_filter = count_filter_ ? 1 : 0;
     b.cell_points = cell_points_;
+    b.warp_min_points = warp_min_points_;
     if (m >= 3)
     {
         launch_frames(p, m, s);

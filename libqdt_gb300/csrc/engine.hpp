@@ -84,6 +84,17 @@ struct DeviceWork;
 // device bytes of a many-set workspace for N points in S sets (batch.cu)
 size_t bcarve_bytes(size_t N, size_t S);
 
+// Process-wide defaults of the schedule knobs, read when a context, batch or
+// server is created (qdtg_set_defaults; the autotuner sets them).
+struct Tuning
+{
+    int cell_points = 0;              // shared-memory cells (0: none)
+    int single_warp_min_points = 512; // single set: nodes of at least this many points merge with a warp
+    int batch_warp_min_points = 512;  // many sets: the same threshold
+    int server_large_workers = 4;     // serving: engines for large requests
+};
+Tuning& tuning();
+
 class Engine
 {
 public:
@@ -122,6 +133,8 @@ public:
     void            set_timing(bool on) { timing_ = on; }
     void            set_cell_points(int c) { cell_points_ = c; }
     int             cell_points() const { return cell_points_; }
+    void            set_warp_min_points(int p) { warp_min_points_ = p; }
+    int             warp_min_points() const { return warp_min_points_; }
 
 private:
     Engine() = default;
@@ -135,6 +148,7 @@ private:
     bool            count_filter_ = false;
     bool            timing_ = false;
     int             cell_points_ = 0;
+    int             warp_min_points_ = 512;
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -163,9 +163,8 @@ __global__ void __launch_bounds__(kCellBlockWarps * 32) k_build_cells(Rec* __res
     build_cell(cell_smem + w * cell_smem_bytes(C), V, R, lo, hi, dc, st, count ? &st->pc : nullptr, out + k);
 }
 
-// Depths with at most this many nodes run one node per warp.
-constexpr long long kWarpNodes = 1 << 12;
-
+// Depths whose nodes have at least b.warp_min_points points run one node per
+// warp, the deeper ones one node per thread.
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 {
     const int nrec = 3 * m;
@@ -191,7 +190,7 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
             k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, s>>>(b.recs, nrec, m, d, b.seam);
             ++launch_counter();
         }
-        if (nodes <= kWarpNodes)
+        if ((m >> d) >= b.warp_min_points)
         {
             const unsigned g = (unsigned)((nodes * 32 + 127) / 128);
             k_build_level<true><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,

@@ -283,12 +283,12 @@ QDT_API void qdtg_server_default_config(qdtg_server_config* c)
 {
     if (!c) return;
     c->hbm_budget_bytes = (size_t)150 << 30;
-    c->large_workers = 4;
+    c->large_workers = qdtg::tuning().server_large_workers;
     c->small_threshold = 65536;
     c->batch_max_points = (size_t)8 << 20;
     c->batch_max_sets = 4096;
     c->max_queue = 4096;
-    c->cell_points = 0;
+    c->cell_points = qdtg::tuning().cell_points;
 }
 
 QDT_API qdtg_server* qdtg_server_create(const qdtg_server_config* config)
