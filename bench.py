@@ -292,9 +292,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform [0,1)^2)",
         "config": {"workload": args.workload, "points": n, "distinct": m, "triangles": ntri,
                    "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "single",
-                   "tuning": ({k: tuning[k] for k in ("cell_points", "single_warp_min_points",
-                                                      "batch_warp_min_points", "server_large_workers")}
-                              if tuning else "defaults")},
+                   "tuning": ({k: tuning[k] for k in autotune.KNOBS} if tuning else "defaults")},
         "exact_violations": viol,
         "stage_ms": {k[3:]: round(v, 4) for k, v in stage_ms.items()},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -63,15 +63,15 @@ QDT_API int qdtg_set_warp_min_points(qdt_t* ptr, int warp_min_points);
 
 /* Process-wide defaults of the schedule knobs, taken by every context, batch
    and server created afterwards (the autotuner of the Python package sets
-   them from its per-GPU cache): shared-memory cell size (0: none), the warp
-   thresholds of the single-set and many-set builds, and the serving
-   engines. A negative value (0 for the last three) keeps the current one.
-   Returns 0 and changes nothing for a value out of range. Call before
+   them from its per-GPU cache): shared-memory cell size of the single-set
+   and of the many-set builds (0: none), their warp thresholds, and the
+   serving engines. A negative value (0 for the last three) keeps the current
+   one. Returns 0 and changes nothing for a value out of range. Call before
    creating contexts; not synchronised with concurrent creation. */
-QDT_API int  qdtg_set_defaults(int cell_points, int single_warp_min_points, int batch_warp_min_points,
-    int server_large_workers);
-QDT_API void qdtg_get_defaults(int* cell_points, int* single_warp_min_points, int* batch_warp_min_points,
-    int* server_large_workers);
+QDT_API int  qdtg_set_defaults(int cell_points, int batch_cell_points, int single_warp_min_points,
+    int batch_warp_min_points, int server_large_workers);
+QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* single_warp_min_points,
+    int* batch_warp_min_points, int* server_large_workers);
 
 /* Fills *info for the last batch call of the context. Returns 1, or 0 when
    ptr or info is NULL. */
@@ -240,7 +240,8 @@ typedef struct qdtg_server_config
     size_t batch_max_points;   /* points per coalesced batch; default 8 Mi */
     size_t batch_max_sets;     /* requests per coalesced batch; default 4096 */
     size_t max_queue;          /* waiting requests beyond which new ones are rejected; default 4096 */
-    int    cell_points;        /* as qdtg_set_cell_points; default 0 */
+    int    cell_points;        /* engines: as qdtg_set_cell_points; default from qdtg_set_defaults */
+    int    batch_cell_points;  /* batching engine: as qdtg_batch_set_cell_points; likewise */
 } qdtg_server_config;
 
 typedef struct qdtg_server_stats

@@ -84,11 +84,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
     lib.qdtg_set_warp_min_points.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_warp_min_points.restype = ctypes.c_int
-    lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 4
+    lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 5
     lib.qdtg_set_defaults.restype = ctypes.c_int
     lib.qdtg_device_name.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.qdtg_device_name.restype = ctypes.c_int
-    lib.qdtg_get_defaults.argtypes = [ctypes.POINTER(ctypes.c_int)] * 4
+    lib.qdtg_get_defaults.argtypes = [ctypes.POINTER(ctypes.c_int)] * 5
     lib.qdtg_get_defaults.restype = None
     lib.qdtg_get_run_info.argtypes = [P, ctypes.POINTER(RunInfo)]
     lib.qdtg_get_run_info.restype = ctypes.c_int

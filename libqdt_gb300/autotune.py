@@ -45,9 +45,12 @@ def _version(lib) -> str:
     return lib.qdtg_version().decode()
 
 
+KNOBS = ("cell_points", "batch_cell_points", "single_warp_min_points", "batch_warp_min_points",
+         "server_large_workers")
+
+
 def apply(lib, cfg: dict) -> bool:
-    return lib.qdtg_set_defaults(int(cfg["cell_points"]), int(cfg["single_warp_min_points"]),
-                                 int(cfg["batch_warp_min_points"]), int(cfg["server_large_workers"])) == 1
+    return lib.qdtg_set_defaults(*[int(cfg[k]) for k in KNOBS]) == 1
 
 
 def load_cached(lib) -> dict | None:
@@ -61,7 +64,7 @@ def load_cached(lib) -> dict | None:
         cfg = json.load(open(path))
     except (OSError, ValueError):
         return None
-    if cfg.get("library") != _version(lib):
+    if cfg.get("library") != _version(lib) or any(k not in cfg for k in KNOBS):
         return None
     return cfg if apply(lib, cfg) else None
 
@@ -106,6 +109,7 @@ def tune(lib, verbose: bool = False) -> dict:
     best_w = min(SINGLE_WARP, key=lambda w: meas["single"]["warp%d_cells0" % w])
     for c in CELLS[1:]:
         meas["single"]["warp%d_cells%d" % (best_w, c)] = single(best_w, c)
+        log("single cells", c, meas["single"]["warp%d_cells%d" % (best_w, c)])
     best_c = min(CELLS, key=lambda c: meas["single"]["warp%d_cells%d" % (best_w, c)])
 
     # many sets: 1,024 sets of the batched workload's distribution
@@ -113,10 +117,10 @@ def tune(lib, verbose: bool = False) -> dict:
     off = G.Batch.offsets_of(sets)
     allpts = np.concatenate(sets)
 
-    def batch(warp):
+    def batch(warp, cells):
         with G.Batch(lib) as b:
             b.set_options(stage_timing=True, use_graphs=False, warp_min_points=warp)
-            b.set_cell_points(best_c)
+            b.set_cell_points(cells)
 
             def run():
                 if b.execute(allpts, off) != 0:
@@ -125,9 +129,13 @@ def tune(lib, verbose: bool = False) -> dict:
             return _best_build_ms(run)
 
     for w in BATCH_WARP:
-        meas["batch"]["warp%d" % w] = batch(w)
-        log("batch warp", w, meas["batch"]["warp%d" % w])
-    best_bw = min(BATCH_WARP, key=lambda w: meas["batch"]["warp%d" % w])
+        meas["batch"]["warp%d_cells0" % w] = batch(w, 0)
+        log("batch warp", w, meas["batch"]["warp%d_cells0" % w])
+    best_bw = min(BATCH_WARP, key=lambda w: meas["batch"]["warp%d_cells0" % w])
+    for c in CELLS[1:]:
+        meas["batch"]["warp%d_cells%d" % (best_bw, c)] = batch(best_bw, c)
+        log("batch cells", c, meas["batch"]["warp%d_cells%d" % (best_bw, c)])
+    best_bc = min(CELLS, key=lambda c: meas["batch"]["warp%d_cells%d" % (best_bw, c)])
 
     # serving engines: throughput of a saturating request stream
     reqs = W.request_stream(48, rate_per_s=2000.0, lo=20_000, hi=1_000_000, seed=103)
@@ -141,7 +149,8 @@ def tune(lib, verbose: bool = False) -> dict:
 
     cfg = {
         "gpu": gpu_name(lib), "library": _version(lib), "date": time.strftime("%Y-%m-%d %H:%M:%S"),
-        "cell_points": best_c, "single_warp_min_points": best_w, "batch_warp_min_points": best_bw,
+        "cell_points": best_c, "batch_cell_points": best_bc, "single_warp_min_points": best_w,
+        "batch_warp_min_points": best_bw,
         "server_large_workers": best_k, "seconds": round(time.time() - t_start, 1),
         "measured": {k: {kk: round(vv, 3) for kk, vv in v.items()} for k, v in meas.items()},
         "units": {"single": "ms build, 1,048,576 uniform", "batch": "ms build, 1,024 sets",

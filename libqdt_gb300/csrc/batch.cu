@@ -1126,7 +1126,7 @@ QDT_API qdtg_batch* qdtg_batch_create(void)
         return nullptr;
     }
     for (auto& ev : e.ev) cudaEventCreate(&ev);
-    e.cell_points = qdtg::tuning().cell_points;
+    e.cell_points = qdtg::tuning().batch_cell_points;
     e.warp_min_points = qdtg::tuning().batch_warp_min_points;
     return b;
 }

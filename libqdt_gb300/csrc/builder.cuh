@@ -578,7 +578,7 @@ using CellBuilder = MapBuilder<CellMap>;
 // A scan that deletes its whole window goes on in another pass, without
 // re-testing validity (builder.hxx:216-222). Record indices are clamped to
 // the pool, so no access leaves it; the loops are bounded by guards.
-constexpr int kWin = 4;
+constexpr int kWin = 2;
 
 struct Ent
 {
@@ -627,9 +627,11 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
     const bool     left = lane < 16;
     const int      j = lane & 15;
     const bool     slot = j < kWin;
-    const bool     combo = j >= 4 && j < 12;
     const int      q = left ? (j - 4) : (j + 4);   // combo index 0..15 = 4 a + b
     const int      ca = q >> 2, rb = q & 3;
+    // lanes 4..11 and 20..27 hold the choice tests of the pairs (a, b) inside
+    // the window (dl, dr < kWin when a pass ends with a choice)
+    const bool     combo = j >= 4 && j < 12 && ca < kWin && rb < kWin;
     const int      jj = slot ? j : 0;               // window slot this lane keeps
 
     int basel = 0;

@@ -360,23 +360,26 @@ QDT_API int qdtg_device_name(char* out, size_t cap)
     return 1;
 }
 
-QDT_API int qdtg_set_defaults(int cell_points, int single_warp_min_points, int batch_warp_min_points,
-    int server_large_workers)
+QDT_API int qdtg_set_defaults(int cell_points, int batch_cell_points, int single_warp_min_points,
+    int batch_warp_min_points, int server_large_workers)
 {
-    if (cell_points > qdtg::kCellMax || (cell_points > 0 && cell_points < 4) || server_large_workers > 64) return 0;
+    auto bad_cells = [](int c) { return c > qdtg::kCellMax || (c > 0 && c < 4); };
+    if (bad_cells(cell_points) || bad_cells(batch_cell_points) || server_large_workers > 64) return 0;
     qdtg::Tuning& t = qdtg::tuning();
     if (cell_points >= 0) t.cell_points = cell_points;
+    if (batch_cell_points >= 0) t.batch_cell_points = batch_cell_points;
     if (single_warp_min_points > 0) t.single_warp_min_points = single_warp_min_points;
     if (batch_warp_min_points > 0) t.batch_warp_min_points = batch_warp_min_points;
     if (server_large_workers > 0) t.server_large_workers = server_large_workers;
     return 1;
 }
 
-QDT_API void qdtg_get_defaults(int* cell_points, int* single_warp_min_points, int* batch_warp_min_points,
-    int* server_large_workers)
+QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* single_warp_min_points,
+    int* batch_warp_min_points, int* server_large_workers)
 {
     const qdtg::Tuning& t = qdtg::tuning();
     if (cell_points) *cell_points = t.cell_points;
+    if (batch_cell_points) *batch_cell_points = t.batch_cell_points;
     if (single_warp_min_points) *single_warp_min_points = t.single_warp_min_points;
     if (batch_warp_min_points) *batch_warp_min_points = t.batch_warp_min_points;
     if (server_large_workers) *server_large_workers = t.server_large_workers;

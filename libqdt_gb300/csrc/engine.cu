@@ -84,6 +84,8 @@ size_t carve(DeviceWork& w, char* base, size_t N)
     p.side = c.take<uint8_t>(N);
     p.seam = c.take<double>((size_t)2 << kSeamDepth);
     b.seam = p.seam;
+    p.box = c.take<unsigned long long>(4);
+    b.box = p.box;
     p.V = c.take<double2>(N);
     p.vid = c.take<uint32_t>(N);
     p.status = c.take<DevStatus>(1);

@@ -88,7 +88,8 @@ size_t bcarve_bytes(size_t N, size_t S);
 // server is created (qdtg_set_defaults; the autotuner sets them).
 struct Tuning
 {
-    int cell_points = 0;              // shared-memory cells (0: none)
+    int cell_points = 0;              // single set: shared-memory cells (0: none)
+    int batch_cell_points = 0;        // many sets: the same
     int single_warp_min_points = 512; // single set: nodes of at least this many points merge with a warp
     int batch_warp_min_points = 512;  // many sets: the same threshold
     int server_large_workers = 4;     // serving: engines for large requests

@@ -31,6 +31,7 @@ struct PrepBuffers
     int            acur = 0, bcur = 0;
     uint8_t*       side = nullptr;      // m
     double*        seam = nullptr;      // 2^(kSeamDepth+1): cut coordinate per upper node
+    unsigned long long* box = nullptr;  // 4: bounding box of the points as order keys (min x, min y, max x, max y)
     double2*       V = nullptr;         // m, leaf order
     uint32_t*      vid = nullptr;       // m
     DevStatus*     status = nullptr;
@@ -50,6 +51,7 @@ struct BuildBuffers
     uint32_t*      tri_count = nullptr; // device word
     DevStatus*     status = nullptr;
     const double*  seam = nullptr;      // cut coordinates of the upper nodes (PrepBuffers::seam)
+    const unsigned long long* box = nullptr;   // PrepBuffers::box
     int            count_filter = 0;    // count filter failures in status
     int            cell_points = 0;     // largest cell built in shared memory (0: no cells)
     int            warp_min_points = 512;   // depths whose nodes have at least this many points: a warp per node

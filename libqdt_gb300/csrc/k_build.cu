@@ -114,10 +114,27 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
 // and their records were last touched by far deeper levels, so without this
 // a bubble step waits on several DRAM round trips. A record lies near a seam
 // when one of its origins is closer to the cut line than 3 times the edge's
-// own length -- the edges a merge walks or deletes around the seam, at the
-// local scale of the point set. The scan reads the records with streaming
-// (evict-first) loads so that it does not displace what it prefetches.
-__global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int d, const double* __restrict__ seam)
+// own length (long edges around the seam, at the local scale of the point
+// set) or than a band of kSeamBand mean point spacings (the short edges at
+// the vertices along the seam, which the candidate windows walk; seam[0]
+// holds the band). Two kernels: the scan reads every record with streaming
+// (evict-first) loads and lists the selected ones; then the list is
+// prefetched, after the stream, so that the stream does not evict it.
+constexpr double kSeamBand = 3.0;
+
+// seam[0] = kSeamBand mean point spacings: sqrt(bounding-box area / m)
+__global__ void k_seam_band(const unsigned long long* __restrict__ box, int m, double* __restrict__ seam)
+{
+    auto val = [](unsigned long long k) {
+        return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+    };
+    const double w = val(box[2]) - val(box[0]), h = val(box[3]) - val(box[1]);
+    const double a = w * h;
+    seam[0] = (m > 0 && a > 0.0 && isfinite(a)) ? kSeamBand * sqrt(a / m) : 0.0;
+}
+
+__global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int d, const double* __restrict__ seam,
+    uint32_t* __restrict__ list, uint32_t* __restrict__ count, uint32_t cap)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
@@ -140,9 +157,20 @@ __global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int
     const double c0 = (d & 1) ? p0.y : p0.x, c1 = (d & 1) ? p1.y : p1.x;
     const double dist = fmin(fabs(c0 - s), fabs(c1 - s));
     const double len = fmax(fabs(p0.x - p1.x), fabs(p0.y - p1.y));
-    if (dist <= 3.0 * len)
+    if (dist <= 3.0 * len || dist <= seam[0])
     {
-        const char* base = reinterpret_cast<const char*>(&R[r]);
+        const uint32_t i = atomicAdd(count, 1u);
+        if (i < cap) list[i] = (uint32_t)r;
+    }
+}
+
+__global__ void k_prefetch_list(const Rec* __restrict__ R, const uint32_t* __restrict__ list,
+    const uint32_t* __restrict__ count, uint32_t cap)
+{
+    const uint32_t n = min(*count, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const char* base = reinterpret_cast<const char*>(&R[list[i]]);
         asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(base));
         asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(base + 32));
     }
@@ -182,13 +210,27 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         ++launch_counter();
         D = dc - 1;
     }
+    const bool prefetch = b.seam && b.box && m >= (1 << 16);
+    if (prefetch)
+    {
+        k_seam_band<<<1, 1, 0, s>>>(b.box, m, const_cast<double*>(b.seam));
+        ++launch_counter();
+    }
     for (int d = D; d >= 0; --d)
     {
         const long long nodes = 1ll << d;
-        if (d <= kSeamDepth && b.seam && m >= (1 << 16))
+        if (d <= kSeamDepth && prefetch)
         {
-            k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, s>>>(b.recs, nrec, m, d, b.seam);
-            ++launch_counter();
+            // the list lives in the extraction's offsets (3 m words, unused
+            // until the extraction) and its length in the triangle counter
+            // (written by the extraction's scan)
+            uint32_t* const list = b.tri_off;
+            uint32_t* const count = b.tri_count;
+            cudaMemsetAsync(count, 0, sizeof(uint32_t), s);
+            k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, s>>>(b.recs, nrec, m, d, b.seam, list, count,
+                (uint32_t)nrec);
+            k_prefetch_list<<<152 * 8, 256, 0, s>>>(b.recs, list, count, (uint32_t)nrec);
+            launch_counter() += 2;
         }
         if ((m >> d) >= b.warp_min_points)
         {

@@ -386,10 +386,52 @@ void launch_split(PrepBuffers& b, int m, cudaStream_t s)
     }
 }
 
+// order-preserving key of a double (larger double, larger key)
+__device__ __forceinline__ unsigned long long box_key(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// bounding box of the distinct points, as order keys: box = {min x, min y,
+// max x, max y}, preset to {~0, ~0, 0, 0}
+__global__ void k_bbox(const double2* __restrict__ P, int m, unsigned long long* __restrict__ box)
+{
+    unsigned long long mnx = ~0ull, mny = ~0ull, mxx = 0, mxy = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    {
+        const double2            p = P[i];
+        const unsigned long long kx = box_key(p.x), ky = box_key(p.y);
+        mnx = min(mnx, kx), mny = min(mny, ky), mxx = max(mxx, kx), mxy = max(mxy, ky);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicMin(&box[0], mnx);
+        atomicMin(&box[1], mny);
+        atomicMax(&box[2], mxx);
+        atomicMax(&box[3], mxy);
+    }
+}
+
 void launch_finalize(const PrepBuffers& b, int m, cudaStream_t s)
 {
     k_finalize<<<grid_for(m, 256), 256, 0, s>>>(b.A[b.acur], b.B[b.bcur], b.ucoord, b.uid, m, b.V, b.vid);
     ++launch_counter();
+    if (b.box)
+    {
+        // the seam prefetch scales its band by the mean point spacing
+        cudaMemsetAsync(b.box, 0xFF, 2 * sizeof(unsigned long long), s);
+        cudaMemsetAsync(b.box + 2, 0x00, 2 * sizeof(unsigned long long), s);
+        k_bbox<<<(unsigned)std::min<size_t>(grid_for(m, 256), 152 * 4), 256, 0, s>>>(b.ucoord, m, b.box);
+        ++launch_counter();
+    }
 }
 
 }  // namespace qdtg

@@ -289,6 +289,7 @@ QDT_API void qdtg_server_default_config(qdtg_server_config* c)
     c->batch_max_sets = 4096;
     c->max_queue = 4096;
     c->cell_points = qdtg::tuning().cell_points;
+    c->batch_cell_points = qdtg::tuning().batch_cell_points;
 }
 
 QDT_API qdtg_server* qdtg_server_create(const qdtg_server_config* config)
@@ -317,7 +318,7 @@ QDT_API qdtg_server* qdtg_server_create(const qdtg_server_config* config)
         return nullptr;
     }
     qdtg_batch_set_options(s.batch, 0, 0, /*graphs: every batch has its own shape*/ 0, 0);
-    qdtg_batch_set_cell_points(s.batch, c.cell_points);
+    qdtg_batch_set_cell_points(s.batch, c.batch_cell_points);
     if (c.small_threshold > 0)
     {
         if (qdtg::bcarve_bytes(std::max<size_t>(c.batch_max_points, 4096), std::max<size_t>(c.batch_max_sets, 64)) >

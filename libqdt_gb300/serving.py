@@ -35,6 +35,7 @@ class ServerConfig(ctypes.Structure):
         ("batch_max_sets", ctypes.c_size_t),
         ("max_queue", ctypes.c_size_t),
         ("cell_points", ctypes.c_int),
+        ("batch_cell_points", ctypes.c_int),
     ]
 
 
