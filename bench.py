@@ -39,6 +39,11 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpoints/s triangulated (0 exact violations), single+batched; p50/p99 latency"
 UNIT = "Mpoints/s"
 
+# DRAM bytes (read + written) of the build launches of one call, measured with
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum over every k_build_level
+# launch of the second of two `--profile-run single` calls, one pass each)
+BUILD_TRAFFIC = {"uniform_2p6m": 2_600_100_000 + 1_043_000_000}
+
 WORKLOADS = {
     "uniform_2p6m": ("uniform", 2600000, 2),
     "uniform_1m": ("uniform", 1048576, 1),
@@ -300,7 +305,9 @@ def run_gb300(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "stage": top[3:], "achieved": round(achieved, 2), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 5),
-                     "traffic": None, "algorithmic_bytes": alg[top]},
+                     "traffic": BUILD_TRAFFIC.get(args.workload) if top == "ms_build" else None,
+                     "traffic_per": "one call's build launches (all depths), ncu dram bytes read + written",
+                     "algorithmic_bytes": alg[top]},
         "clocks": ck,
     }
     if rank == 0 and not args.no_cpu_baseline:
