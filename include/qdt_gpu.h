@@ -55,23 +55,26 @@ QDT_API size_t qdtg_workspace_bytes(size_t n);
    returns 0 (and an empty string) when no device is usable. */
 QDT_API int qdtg_device_name(char* out, size_t cap);
 
-/* The smallest node (points) that the context's build merges with a whole
-   warp instead of one thread (default 512). Returns 1, or 0 for a NULL
-   context, a value below 1 or no usable GPU. The triangulation does not
-   depend on it. */
-QDT_API int qdtg_set_warp_min_points(qdt_t* ptr, int warp_min_points);
+/* The context's build merges with a whole warp per node at the depths that
+   have at most warp_nodes nodes (few merges: each one's latency counts) and
+   with one thread per node below (many merges); default 4096. Returns 1, or
+   0 for a NULL context, a value below 1 or no usable GPU. The triangulation
+   does not depend on it. */
+QDT_API int qdtg_set_warp_nodes(qdt_t* ptr, int warp_nodes);
 
 /* Process-wide defaults of the schedule knobs, taken by every context, batch
    and server created afterwards (the autotuner of the Python package sets
    them from its per-GPU cache): shared-memory cell size of the single-set
-   and of the many-set builds (0: none), their warp thresholds, and the
-   serving engines. A negative value (0 for the last three) keeps the current
-   one. Returns 0 and changes nothing for a value out of range. Call before
-   creating contexts; not synchronised with concurrent creation. */
-QDT_API int  qdtg_set_defaults(int cell_points, int batch_cell_points, int single_warp_min_points,
-    int batch_warp_min_points, int server_large_workers);
-QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* single_warp_min_points,
-    int* batch_warp_min_points, int* server_large_workers);
+   and of the many-set builds (0: none), the single-set warp threshold
+   (qdtg_set_warp_nodes), the many-set thresholds (qdtg_batch_set_options,
+   qdtg_batch_set_warp_nodes) and the serving engines. A negative value (0
+   for the last four) keeps the current one. Returns 0 and changes nothing
+   for a value out of range. Call before creating contexts; not synchronised
+   with concurrent creation. */
+QDT_API int  qdtg_set_defaults(int cell_points, int batch_cell_points, int single_warp_nodes,
+    int batch_warp_min_points, int batch_warp_nodes, int server_large_workers);
+QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* single_warp_nodes,
+    int* batch_warp_min_points, int* batch_warp_nodes, int* server_large_workers);
 
 /* Fills *info for the last batch call of the context. Returns 1, or 0 when
    ptr or info is NULL. */
@@ -206,6 +209,11 @@ QDT_API size_t qdtg_batch_download_device_triangles(const qdtg_batch* b, uint32_
    node per thread (0 keeps the current value; default 512). */
 QDT_API void qdtg_batch_set_options(qdtg_batch* b, int count_filter_failures, int stage_timing, int use_graphs,
     int warp_min_points);
+/* The heights (node sizes) merged with a warp per node are those whose nodes
+   have at least warp_min_points points (qdtg_batch_set_options) or whose
+   launch has at most warp_nodes nodes (default 4096). Returns 1, or 0 for a
+   NULL batch or a negative value. */
+QDT_API int qdtg_batch_set_warp_nodes(qdtg_batch* b, int warp_nodes);
 /* The largest subtree (points, 4..1024; 0 = none) built in shared memory,
    as qdtg_set_cell_points(). Returns 1, or 0 for a bad value. */
 QDT_API int   qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points);

@@ -22,7 +22,8 @@ from .qdt_api import (QDT_OK, QDT_ERR_NULL_CONTEXT, QDT_ERR_NULL_ARGUMENT, QDT_E
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
-GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_min_points", "qdtg_set_defaults",
+GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_nodes", "qdtg_set_defaults",
+               "qdtg_batch_set_warp_nodes",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -82,13 +83,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_cell_points.restype = ctypes.c_int
     lib.qdtg_workspace_bytes.argtypes = [ctypes.c_size_t]
     lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
-    lib.qdtg_set_warp_min_points.argtypes = [P, ctypes.c_int]
-    lib.qdtg_set_warp_min_points.restype = ctypes.c_int
-    lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 5
+    lib.qdtg_set_warp_nodes.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_warp_nodes.restype = ctypes.c_int
+    lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 6
     lib.qdtg_set_defaults.restype = ctypes.c_int
     lib.qdtg_device_name.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.qdtg_device_name.restype = ctypes.c_int
-    lib.qdtg_get_defaults.argtypes = [ctypes.POINTER(ctypes.c_int)] * 5
+    lib.qdtg_get_defaults.argtypes = [ctypes.POINTER(ctypes.c_int)] * 6
     lib.qdtg_get_defaults.restype = None
     lib.qdtg_get_run_info.argtypes = [P, ctypes.POINTER(RunInfo)]
     lib.qdtg_get_run_info.restype = ctypes.c_int
@@ -132,6 +133,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             ("qdtg_batch_download_device_triangles", [P, P, S, P], S),
             ("qdtg_batch_set_options", [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], None),
             ("qdtg_batch_set_cell_points", [P, ctypes.c_int], ctypes.c_int),
+            ("qdtg_batch_set_warp_nodes", [P, ctypes.c_int], ctypes.c_int),
             ("qdtg_batch_reserve", [P, S, S], ctypes.c_int),
             ("qdtg_batch_workspace_bytes", [P], S),
             ("qdtg_batch_get_run_info", [P, ctypes.POINTER(RunInfo)], ctypes.c_int),
@@ -187,8 +189,8 @@ class Triangulation(qdt_api.Context):
     def set_cell_points(self, cell_points: int) -> bool:
         return self.lib.qdtg_set_cell_points(self.ptr, int(cell_points)) == 1
 
-    def set_warp_min_points(self, points: int) -> bool:
-        return self.lib.qdtg_set_warp_min_points(self.ptr, int(points)) == 1
+    def set_warp_nodes(self, nodes: int) -> bool:
+        return self.lib.qdtg_set_warp_nodes(self.ptr, int(nodes)) == 1
 
     def execute_device(self, d_ptr: int, n: int, stream: int = 0) -> int:
         return self.lib.qdtg_execute_device(self.ptr, d_ptr, n, stream or None)
@@ -313,6 +315,9 @@ class Batch:
 
     def set_cell_points(self, cell_points: int) -> bool:
         return self.lib.qdtg_batch_set_cell_points(self.ptr, int(cell_points)) == 1
+
+    def set_warp_nodes(self, nodes: int) -> bool:
+        return self.lib.qdtg_batch_set_warp_nodes(self.ptr, int(nodes)) == 1
 
     def stream(self) -> int:
         return self.lib.qdtg_batch_stream(self.ptr) or 0

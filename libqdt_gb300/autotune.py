@@ -25,8 +25,9 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE_DIR = os.path.join(HERE, "_build")
 
-SINGLE_WARP = (256, 512, 1024, 2048)
-BATCH_WARP = (256, 512, 1024, 2048)
+SINGLE_WARP_NODES = (1024, 2048, 4096, 8192)
+BATCH_WARP_POINTS = (256, 512, 1024)
+BATCH_WARP_NODES = (1024, 4096, 16384)
 CELLS = (0, 128)
 WORKERS = (2, 4, 8)
 
@@ -45,7 +46,7 @@ def _version(lib) -> str:
     return lib.qdtg_version().decode()
 
 
-KNOBS = ("cell_points", "batch_cell_points", "single_warp_min_points", "batch_warp_min_points",
+KNOBS = ("cell_points", "batch_cell_points", "single_warp_nodes", "batch_warp_min_points", "batch_warp_nodes",
          "server_large_workers")
 
 
@@ -88,54 +89,69 @@ def tune(lib, verbose: bool = False) -> dict:
         if verbose:
             print("autotune:", *a, flush=True)
 
-    # single set: 1,048,576 uniform points
-    pts = W.uniform(1 << 20, 101)
+    # single set: one large set (1,048,576 uniform points, throughput) and
+    # 16 small ones (2,000 points, latency); the cost is the sum of builds
+    singles = [W.uniform(1 << 20, 101)] + [W.uniform(2000, 200 + i) for i in range(16)]
 
-    def single(warp, cells):
+    def single(nodes, cells):
         with G.Triangulation(lib) as t:
             t.set_options(stage_timing=True)
-            t.set_warp_min_points(warp)
+            t.set_warp_nodes(nodes)
             t.set_cell_points(cells)
 
             def run():
-                if t.execute(pts) != 0:
-                    raise RuntimeError("qdt_execute failed during tuning")
-                return t.run_info()["ms_build"]
+                total = 0.0
+                for p in singles:
+                    if t.execute(p) != 0:
+                        raise RuntimeError("qdt_execute failed during tuning")
+                    total += t.run_info()["ms_build"]
+                return total
             return _best_build_ms(run)
 
-    for w in SINGLE_WARP:
-        meas["single"]["warp%d_cells0" % w] = single(w, 0)
-        log("single warp", w, meas["single"]["warp%d_cells0" % w])
-    best_w = min(SINGLE_WARP, key=lambda w: meas["single"]["warp%d_cells0" % w])
+    for w in SINGLE_WARP_NODES:
+        meas["single"]["nodes%d_cells0" % w] = single(w, 0)
+        log("single warp nodes", w, meas["single"]["nodes%d_cells0" % w])
+    best_w = min(SINGLE_WARP_NODES, key=lambda w: meas["single"]["nodes%d_cells0" % w])
     for c in CELLS[1:]:
-        meas["single"]["warp%d_cells%d" % (best_w, c)] = single(best_w, c)
-        log("single cells", c, meas["single"]["warp%d_cells%d" % (best_w, c)])
-    best_c = min(CELLS, key=lambda c: meas["single"]["warp%d_cells%d" % (best_w, c)])
+        meas["single"]["nodes%d_cells%d" % (best_w, c)] = single(best_w, c)
+        log("single cells", c, meas["single"]["nodes%d_cells%d" % (best_w, c)])
+    best_c = min(CELLS, key=lambda c: meas["single"]["nodes%d_cells%d" % (best_w, c)])
 
     # many sets: 1,024 sets of the batched workload's distribution
-    sets = W.many_sets(count=1024, lo=16, hi=65536, seed=102)
-    off = G.Batch.offsets_of(sets)
-    allpts = np.concatenate(sets)
+    # (throughput) and 16 sets of 4,000 points (latency, like a coalesced
+    # serving batch)
+    batches = []
+    for sets in (W.many_sets(count=1024, lo=16, hi=65536, seed=102),
+                 [W.uniform(4000, 300 + i) for i in range(16)]):
+        batches.append((np.concatenate(sets), G.Batch.offsets_of(sets)))
 
-    def batch(warp, cells):
+    def batch(points, nodes, cells):
         with G.Batch(lib) as b:
-            b.set_options(stage_timing=True, use_graphs=False, warp_min_points=warp)
+            b.set_options(stage_timing=True, use_graphs=False, warp_min_points=points)
+            b.set_warp_nodes(nodes)
             b.set_cell_points(cells)
 
             def run():
-                if b.execute(allpts, off) != 0:
-                    raise RuntimeError("qdtg_batch_execute failed during tuning")
-                return b.run_info()["ms_build"]
+                total = 0.0
+                for allpts, off in batches:
+                    if b.execute(allpts, off) != 0:
+                        raise RuntimeError("qdtg_batch_execute failed during tuning")
+                    total += b.run_info()["ms_build"]
+                return total
             return _best_build_ms(run)
 
-    for w in BATCH_WARP:
-        meas["batch"]["warp%d_cells0" % w] = batch(w, 0)
-        log("batch warp", w, meas["batch"]["warp%d_cells0" % w])
-    best_bw = min(BATCH_WARP, key=lambda w: meas["batch"]["warp%d_cells0" % w])
+    for pw in BATCH_WARP_POINTS:
+        for nw in BATCH_WARP_NODES:
+            key = "points%d_nodes%d_cells0" % (pw, nw)
+            meas["batch"][key] = batch(pw, nw, 0)
+            log("batch", key, meas["batch"][key])
+    best_bw, best_bn = min(((pw, nw) for pw in BATCH_WARP_POINTS for nw in BATCH_WARP_NODES),
+                           key=lambda x: meas["batch"]["points%d_nodes%d_cells0" % x])
     for c in CELLS[1:]:
-        meas["batch"]["warp%d_cells%d" % (best_bw, c)] = batch(best_bw, c)
-        log("batch cells", c, meas["batch"]["warp%d_cells%d" % (best_bw, c)])
-    best_bc = min(CELLS, key=lambda c: meas["batch"]["warp%d_cells%d" % (best_bw, c)])
+        key = "points%d_nodes%d_cells%d" % (best_bw, best_bn, c)
+        meas["batch"][key] = batch(best_bw, best_bn, c)
+        log("batch", key, meas["batch"][key])
+    best_bc = min(CELLS, key=lambda c: meas["batch"]["points%d_nodes%d_cells%d" % (best_bw, best_bn, c)])
 
     # serving engines: throughput of a saturating request stream
     reqs = W.request_stream(48, rate_per_s=2000.0, lo=20_000, hi=1_000_000, seed=103)
@@ -149,11 +165,12 @@ def tune(lib, verbose: bool = False) -> dict:
 
     cfg = {
         "gpu": gpu_name(lib), "library": _version(lib), "date": time.strftime("%Y-%m-%d %H:%M:%S"),
-        "cell_points": best_c, "batch_cell_points": best_bc, "single_warp_min_points": best_w,
-        "batch_warp_min_points": best_bw,
+        "cell_points": best_c, "batch_cell_points": best_bc, "single_warp_nodes": best_w,
+        "batch_warp_min_points": best_bw, "batch_warp_nodes": best_bn,
         "server_large_workers": best_k, "seconds": round(time.time() - t_start, 1),
         "measured": {k: {kk: round(vv, 3) for kk, vv in v.items()} for k, v in meas.items()},
-        "units": {"single": "ms build, 1,048,576 uniform", "batch": "ms build, 1,024 sets",
+        "units": {"single": "ms build, 1,048,576 uniform + 16 x 2,000",
+                  "batch": "ms build, 1,024 sets + 16 sets of 4,000",
                   "serving": "Mpts/s, 48 requests 2e4..1e6 points"},
     }
     os.makedirs(CACHE_DIR, exist_ok=True)

@@ -538,7 +538,8 @@ struct BatchEngine
     bool                  host_results = false;   // h_tris and h_rep hold the last call's results
     RunInfo               info;
     bool                  count_filter = false, timing = false, use_graph = true;
-    int                   warp_min_points = 512;   // nodes of at least this many points merge with a warp each
+    int                   warp_min_points = 512;   // heights whose nodes have at least this many points: a warp per node
+    int                   warp_nodes = 4096;       // heights with at most this many nodes: a warp per node
     int                   cell_points = 0;         // largest cell built in shared memory (0: none)
     std::vector<uint32_t> h_cell_off;
     uint32_t              ncells = 0;
@@ -568,9 +569,13 @@ struct BatchEngine
 
     int ensure(size_t N, size_t S);
     int run(size_t N, size_t S, bool host_io);
-    // nodes of height h have more than 3 * 2^(h-1) points: a warp per node when
-    // that reaches warp_min_points
-    bool height_warp(int h) const { return h >= 1 && 3ll * (1ll << (h - 1)) + 1 >= warp_min_points; }
+    // a warp per node at height h >= 1 when its nodes are large (they have more
+    // than 3 * 2^(h-1) points) or few (the launch is then bound by the
+    // latency of each merge, not by throughput)
+    bool height_warp(int h, long long nodes) const
+    {
+        return h >= 1 && (3ll * (1ll << (h - 1)) + 1 >= warp_min_points || nodes <= warp_nodes);
+    }
     void post_sync_work(size_t N, size_t S, uint32_t M, int Dmax);
 };
 
@@ -750,7 +755,7 @@ void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax)
         if (h == 0)
             k_bbuild_height<false, true><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes, noff,
                 en, eo, nent, u_off, h, status, cf);
-        else if (height_warp(h))
+        else if (height_warp(h, slots))
             k_bbuild_height<true, false><<<(unsigned)((slots * 32 + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes,
                 noff, en, eo, nent, u_off, h, status, cf);
         else
@@ -910,6 +915,7 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
     mix(count_filter);
     mix(timing);
     mix((uint64_t)warp_min_points);
+    mix((uint64_t)warp_nodes);
     mix((uint64_t)cell_points);
     for (size_t i = 0; i <= S; ++i) mix(h_u_off[i]);
     for (size_t i = 0; i < S; ++i) mix(skipv[i]);
@@ -1128,6 +1134,7 @@ QDT_API qdtg_batch* qdtg_batch_create(void)
     for (auto& ev : e.ev) cudaEventCreate(&ev);
     e.cell_points = qdtg::tuning().batch_cell_points;
     e.warp_min_points = qdtg::tuning().batch_warp_min_points;
+    e.warp_nodes = qdtg::tuning().batch_warp_nodes;
     return b;
 }
 
@@ -1228,6 +1235,13 @@ QDT_API size_t qdtg_batch_workspace_bytes(const qdtg_batch* b)
 {
     if (!b || !b->e.block) return 0;
     return qdtg::bcarve_bytes(b->e.capN, b->e.capS);
+}
+
+QDT_API int qdtg_batch_set_warp_nodes(qdtg_batch* b, int warp_nodes)
+{
+    if (!b || warp_nodes < 0) return 0;
+    b->e.warp_nodes = warp_nodes;
+    return 1;
 }
 
 QDT_API int qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points)

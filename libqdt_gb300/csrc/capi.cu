@@ -360,37 +360,39 @@ QDT_API int qdtg_device_name(char* out, size_t cap)
     return 1;
 }
 
-QDT_API int qdtg_set_defaults(int cell_points, int batch_cell_points, int single_warp_min_points,
-    int batch_warp_min_points, int server_large_workers)
+QDT_API int qdtg_set_defaults(int cell_points, int batch_cell_points, int single_warp_nodes,
+    int batch_warp_min_points, int batch_warp_nodes, int server_large_workers)
 {
     auto bad_cells = [](int c) { return c > qdtg::kCellMax || (c > 0 && c < 4); };
     if (bad_cells(cell_points) || bad_cells(batch_cell_points) || server_large_workers > 64) return 0;
     qdtg::Tuning& t = qdtg::tuning();
     if (cell_points >= 0) t.cell_points = cell_points;
     if (batch_cell_points >= 0) t.batch_cell_points = batch_cell_points;
-    if (single_warp_min_points > 0) t.single_warp_min_points = single_warp_min_points;
+    if (single_warp_nodes > 0) t.single_warp_nodes = single_warp_nodes;
     if (batch_warp_min_points > 0) t.batch_warp_min_points = batch_warp_min_points;
+    if (batch_warp_nodes > 0) t.batch_warp_nodes = batch_warp_nodes;
     if (server_large_workers > 0) t.server_large_workers = server_large_workers;
     return 1;
 }
 
-QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* single_warp_min_points,
-    int* batch_warp_min_points, int* server_large_workers)
+QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* single_warp_nodes,
+    int* batch_warp_min_points, int* batch_warp_nodes, int* server_large_workers)
 {
     const qdtg::Tuning& t = qdtg::tuning();
     if (cell_points) *cell_points = t.cell_points;
     if (batch_cell_points) *batch_cell_points = t.batch_cell_points;
-    if (single_warp_min_points) *single_warp_min_points = t.single_warp_min_points;
+    if (single_warp_nodes) *single_warp_nodes = t.single_warp_nodes;
     if (batch_warp_min_points) *batch_warp_min_points = t.batch_warp_min_points;
+    if (batch_warp_nodes) *batch_warp_nodes = t.batch_warp_nodes;
     if (server_large_workers) *server_large_workers = t.server_large_workers;
 }
 
-QDT_API int qdtg_set_warp_min_points(qdt_t* ptr, int warp_min_points)
+QDT_API int qdtg_set_warp_nodes(qdt_t* ptr, int warp_nodes)
 {
     Context* c = ctx(ptr);
-    if (!c || warp_min_points < 1) return 0;
+    if (!c || warp_nodes < 1) return 0;
     if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
-    c->engine->set_warp_min_points(warp_min_points);
+    c->engine->set_warp_nodes(warp_nodes);
     return 1;
 }
 

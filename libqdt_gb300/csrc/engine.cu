@@ -125,7 +125,7 @@ Engine* Engine::create(int* cuda_error)
     if (!g) return nullptr;
     g->device_ = dev;
     g->cell_points_ = tuning().cell_points;
-    g->warp_min_points_ = tuning().single_warp_min_points;
+    g->warp_nodes_ = tuning().single_warp_nodes;
     if (cudaStreamCreateWithFlags(&g->stream_, cudaStreamNonBlocking) != cudaSuccess)
     {
         cudaGetLastError();
@@ -260,7 +260,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     info_.unique_points = m;
     b.count_filter = count_filter_ ? 1 : 0;
     b.cell_points = cell_points_;
-    b.warp_min_points = warp_min_points_;
+    b.warp_nodes = warp_nodes_;
     if (m >= 3)
     {
         launch_frames(p, m, s);

@@ -90,8 +90,9 @@ struct Tuning
 {
     int cell_points = 0;              // single set: shared-memory cells (0: none)
     int batch_cell_points = 0;        // many sets: the same
-    int single_warp_min_points = 512; // single set: nodes of at least this many points merge with a warp
-    int batch_warp_min_points = 512;  // many sets: the same threshold
+    int single_warp_nodes = 4096;     // single set: depths of at most this many nodes merge with a warp per node
+    int batch_warp_min_points = 512;  // many sets: heights whose nodes have at least this many points, a warp per node
+    int batch_warp_nodes = 4096;      // many sets: also heights with at most this many nodes
     int server_large_workers = 4;     // serving: engines for large requests
 };
 Tuning& tuning();
@@ -134,8 +135,8 @@ public:
     void            set_timing(bool on) { timing_ = on; }
     void            set_cell_points(int c) { cell_points_ = c; }
     int             cell_points() const { return cell_points_; }
-    void            set_warp_min_points(int p) { warp_min_points_ = p; }
-    int             warp_min_points() const { return warp_min_points_; }
+    void            set_warp_nodes(int n) { warp_nodes_ = n; }
+    int             warp_nodes() const { return warp_nodes_; }
 
 private:
     Engine() = default;
@@ -149,7 +150,7 @@ private:
     bool            count_filter_ = false;
     bool            timing_ = false;
     int             cell_points_ = 0;
-    int             warp_min_points_ = 512;
+    int             warp_nodes_ = 4096;
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -54,7 +54,7 @@ struct BuildBuffers
     const unsigned long long* box = nullptr;   // PrepBuffers::box
     int            count_filter = 0;    // count filter failures in status
     int            cell_points = 0;     // largest cell built in shared memory (0: no cells)
-    int            warp_min_points = 512;   // depths whose nodes have at least this many points: a warp per node
+    int            warp_nodes = 4096;   // depths with at most this many nodes: a warp per node
 };
 
 size_t sort_count_words(size_t n);

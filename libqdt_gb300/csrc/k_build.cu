@@ -191,8 +191,9 @@ __global__ void __launch_bounds__(kCellBlockWarps * 32) k_build_cells(Rec* __res
     build_cell(cell_smem + w * cell_smem_bytes(C), V, R, lo, hi, dc, st, count ? &st->pc : nullptr, out + k);
 }
 
-// Depths whose nodes have at least b.warp_min_points points run one node per
-// warp, the deeper ones one node per thread.
+// Depths with at most b.warp_nodes nodes run one node per warp (few merges:
+// the latency of each merge matters), the deeper ones one node per thread
+// (many merges: throughput).
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 {
     const int nrec = 3 * m;
@@ -232,7 +233,7 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
             k_prefetch_list<<<152 * 8, 256, 0, s>>>(b.recs, list, count, (uint32_t)nrec);
             launch_counter() += 2;
         }
-        if ((m >> d) >= b.warp_min_points)
+        if ((1ll << d) <= b.warp_nodes)
         {
             const unsigned g = (unsigned)((nodes * 32 + 127) / 128);
             k_build_level<true><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,

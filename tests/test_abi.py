@@ -97,18 +97,19 @@ def test_version(lib):
 def test_schedule_defaults(lib):
     """qdtg_set_defaults / qdtg_get_defaults: the autotuner's interface."""
     def get():
-        a = [ctypes.c_int() for _ in range(5)]
+        a = [ctypes.c_int() for _ in range(6)]
         lib.qdtg_get_defaults(*[ctypes.byref(x) for x in a])
         return [x.value for x in a]
     old = get()
+    want = [64, 128, 1024, 256, 8192, 2]
     try:
-        assert lib.qdtg_set_defaults(64, 128, 1024, 256, 2) == 1
-        assert get() == [64, 128, 1024, 256, 2]
-        assert lib.qdtg_set_defaults(-1, -1, 0, 0, 0) == 1 and get() == [64, 128, 1024, 256, 2]   # keep
-        assert lib.qdtg_set_defaults(3, -1, 0, 0, 0) == 0 and get() == [64, 128, 1024, 256, 2]    # cells < 4
-        assert lib.qdtg_set_defaults(-1, 2048, 0, 0, 0) == 0                                      # cells > 1024
-        assert lib.qdtg_set_defaults(-1, -1, 0, 0, 65) == 0                                       # > 64 engines
-        assert lib.qdtg_set_defaults(0, 0, 0, 0, 0) == 1 and get()[:2] == [0, 0]                  # cells off
+        assert lib.qdtg_set_defaults(*want) == 1
+        assert get() == want
+        assert lib.qdtg_set_defaults(-1, -1, 0, 0, 0, 0) == 1 and get() == want    # keep
+        assert lib.qdtg_set_defaults(3, -1, 0, 0, 0, 0) == 0 and get() == want     # cells < 4
+        assert lib.qdtg_set_defaults(-1, 2048, 0, 0, 0, 0) == 0                    # cells > 1024
+        assert lib.qdtg_set_defaults(-1, -1, 0, 0, 0, 65) == 0                     # > 64 engines
+        assert lib.qdtg_set_defaults(0, 0, 0, 0, 0, 0) == 1 and get()[:2] == [0, 0]   # cells off
     finally:
         lib.qdtg_set_defaults(*old)
     assert get() == old

@@ -93,6 +93,12 @@ def test_graphs_off_and_timing_same_result(lib):
         check_batch(b, sets)
         info = b.run_info()
         assert info["ms_build"] > 0 and info["ms_total"] > 0
+        # warp merges at every height, then at none
+        for points, nodes in ((1 << 30, 1 << 30), (1 << 30, 0)):
+            b.set_options(use_graphs=True, warp_min_points=points)
+            assert b.set_warp_nodes(nodes)
+            assert b.execute_sets(sets) == Q.QDT_OK
+            check_batch(b, sets)
 
 
 @pytest.mark.parametrize("cells", [0, 4, 33, 128, 1024])
