@@ -55,6 +55,13 @@ QDT_API size_t qdtg_workspace_bytes(size_t n);
    returns 0 (and an empty string) when no device is usable. */
 QDT_API int qdtg_device_name(char* out, size_t cap);
 
+/* The first insertion or constraint after a batch call builds the context's
+   half-edge mesh; with on_gpu != 0 (the default) it is built on the GPU from
+   the batch result the device still holds, else on the host. The mesh and
+   every later result are the same either way. Returns 1, or 0 for a NULL
+   context. */
+QDT_API int qdtg_set_mesh_on_gpu(qdt_t* ptr, int on_gpu);
+
 /* The context's build merges with a whole warp per node at the depths that
    have at most warp_nodes nodes (few merges: each one's latency counts) and
    with one thread per node below (many merges); default 4096. Returns 1, or

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
 GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_nodes", "qdtg_set_defaults",
-               "qdtg_batch_set_warp_nodes",
+               "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -85,6 +85,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
     lib.qdtg_set_warp_nodes.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_warp_nodes.restype = ctypes.c_int
+    lib.qdtg_set_mesh_on_gpu.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_mesh_on_gpu.restype = ctypes.c_int
     lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 6
     lib.qdtg_set_defaults.restype = ctypes.c_int
     lib.qdtg_device_name.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -191,6 +193,9 @@ class Triangulation(qdt_api.Context):
 
     def set_warp_nodes(self, nodes: int) -> bool:
         return self.lib.qdtg_set_warp_nodes(self.ptr, int(nodes)) == 1
+
+    def set_mesh_on_gpu(self, on_gpu: bool) -> bool:
+        return self.lib.qdtg_set_mesh_on_gpu(self.ptr, int(bool(on_gpu))) == 1
 
     def execute_device(self, d_ptr: int, n: int, stream: int = 0) -> int:
         return self.lib.qdtg_execute_device(self.ptr, d_ptr, n, stream or None)

@@ -387,6 +387,14 @@ QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* si
     if (server_large_workers) *server_large_workers = t.server_large_workers;
 }
 
+QDT_API int qdtg_set_mesh_on_gpu(qdt_t* ptr, int on_gpu)
+{
+    Context* c = ctx(ptr);
+    if (!c) return 0;
+    c->mesh_on_gpu = on_gpu != 0;
+    return 1;
+}
+
 QDT_API int qdtg_set_warp_nodes(qdt_t* ptr, int warp_nodes)
 {
     Context* c = ctx(ptr);

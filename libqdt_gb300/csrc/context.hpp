@@ -26,6 +26,7 @@ struct Context
     Engine*             engine = nullptr;
     int                 last_cuda_error = 0;
     Mesh*               mesh = nullptr;    // built on the first insertion or constraint
+    bool                mesh_on_gpu = true;   // build that mesh on the GPU when the engine holds the result
 
     size_t npoints() const { return points.size() / 2; }
     size_t ntris() const { return tris.size() / 3; }

@@ -232,6 +232,17 @@ int Engine::ensure(size_t n)
     return S_OK;
 }
 
+int Engine::build_mesh(size_t n, size_t T, MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h)
+{
+    if (!mesh_source_ || n != mesh_n_ || T != mesh_t_ || !w_ || !w_->block) return -1;
+    if (cudaSetDevice(device_) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return -1;
+    }
+    return mesh_build_device(w_->build.tris, w_->pts, n, T, stream_, o2l, v, h);
+}
+
 const uint32_t* Engine::device_triangles() const { return w_ ? w_->build.tris : nullptr; }
 const uint32_t* Engine::device_rep() const { return w_ ? w_->prep.rep : nullptr; }
 
@@ -323,6 +334,7 @@ int Engine::run_host(const double* xy, size_t n, PinnedVec<double>& points, Pinn
         cudaGetLastError();
         return S_INTERNAL;
     }
+    mesh_source_ = false;
     int st = ensure(n);
     if (st != S_OK) return st;
     // host copies the caller's points into the context (pinned) in chunks; the
@@ -352,11 +364,17 @@ int Engine::run_host(const double* xy, size_t n, PinnedVec<double>& points, Pinn
     *ntri = info_.ntri;
     *unique_points = info_.unique_points;
     tris.resize(3 * info_.ntri);
+    // the points and triangles stay on the device until the next call: the
+    // first insertion or constraint builds its mesh from them
+    mesh_source_ = true;
+    mesh_n_ = n;
+    mesh_t_ = info_.ntri;
     return S_OK;
 }
 
 int Engine::run_device(const double* d_xy, size_t n, cudaStream_t user_stream)
 {
+    mesh_source_ = false;
     if (cudaSetDevice(device_) != cudaSuccess)
     {
         cudaGetLastError();

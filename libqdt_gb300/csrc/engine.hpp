@@ -11,6 +11,8 @@
 
 #include <cuda_runtime.h>
 
+#include "mesh_layout.hpp"
+
 namespace qdtg {
 
 // Allocator for host buffers that the GPU copies to and from: page-locked
@@ -125,6 +127,12 @@ public:
     // frees the workspace (the next call allocates it again)
     void          release_workspace();
 
+    // The half-edge mesh of the last run_host result (n points, T triangles),
+    // built on the device (k_mesh.cu). Returns 0, or a negative value when
+    // the device no longer holds that result or the build failed (the caller
+    // then builds the mesh on the host).
+    int build_mesh(size_t n, size_t T, MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h);
+
     const uint32_t* device_triangles() const;
     const uint32_t* device_rep() const;
     size_t          last_ntri() const { return info_.ntri; }
@@ -151,6 +159,8 @@ private:
     bool            timing_ = false;
     int             cell_points_ = 0;
     int             warp_nodes_ = 4096;
+    bool            mesh_source_ = false;   // the device holds the last run_host's points and triangles
+    size_t          mesh_n_ = 0, mesh_t_ = 0;
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -5,9 +5,11 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "mesh_layout.hpp"
 
 namespace qdtg {
 
@@ -66,6 +68,11 @@ void launch_unique(const PrepBuffers& b, size_t n, cudaStream_t s);
 void launch_frames(PrepBuffers& b, size_t m, cudaStream_t s);
 void launch_split(PrepBuffers& b, int m, cudaStream_t s);
 void launch_finalize(const PrepBuffers& b, int m, cudaStream_t s);
+
+// the half-edge mesh of T triangles (3 T point indices) over n points, both on
+// the device, into host arrays (k_mesh.cu); 0 or a negative value
+int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t T, cudaStream_t s,
+    MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h);
 
 // builds every level from the deepest to the root
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s);

@@ -24,33 +24,21 @@
 #include <vector>
 
 #include "context.hpp"
+#include "mesh_layout.hpp"
 #include "predicates.cuh"
 #include "qdt.h"
 
 namespace qdtg {
 
-struct MV
-{
-    double   x, y;
-    uint32_t orig;
-    int      he;   // an outgoing half-edge
-};
-
-struct HE
-{
-    int  org;
-    int  twin;
-    int  next;
-    int  tri;
-    bool cons;
-};
+using MV = MeshVertex;
+using HE = MeshHalfEdge;
 
 struct Mesh
 {
-    std::vector<MV>  v;
-    std::vector<HE>  h;
+    MeshVec<MV>      v;
+    MeshVec<HE>      h;
     std::vector<int> free_h;
-    std::vector<int> o2l;    // point index -> mesh vertex, -1 when none
+    MeshVec<int>     o2l;    // point index -> mesh vertex, -1 when none
     std::vector<int> t2h;    // triangle -> one of its half-edges
     int              last = 0;
 };
@@ -131,6 +119,20 @@ void build_mesh(Context& c, Mesh& M)
     }
 }
 
+// The same mesh built on the GPU from the batch result the engine still
+// holds (k_mesh.cu); false when it cannot (then the host builds it).
+bool build_mesh_on_device(Context& c, Mesh& M)
+{
+    if (!c.mesh_on_gpu || !c.engine) return false;
+    const size_t T = c.ntris();
+    if (c.engine->build_mesh(c.npoints(), T, M.o2l, M.v, M.h) != 0) return false;
+    M.free_h.clear();
+    M.last = 0;
+    M.t2h.resize(T);
+    for (size_t t = 0; t < T; ++t) M.t2h[t] = (int)(3 * t);
+    return true;
+}
+
 Mesh& ensure_mesh(Context& c)
 {
     if (!c.mesh)
@@ -138,7 +140,7 @@ Mesh& ensure_mesh(Context& c)
         Mesh* m = new Mesh();
         try
         {
-            build_mesh(c, *m);
+            if (!build_mesh_on_device(c, *m)) build_mesh(c, *m);
         }
         catch (...)
         {
@@ -542,7 +544,7 @@ int mesh_insert_point(Context& c, double x, double y, bool)
             if (!(twt >= 0 && in_cav(twt)))
             {
                 const int a = M.h[e].org, b = M.h[M.h[e].next].org;
-                if (tw >= 0 || orient(M, a, b, x, y) > 0) bnd.push_back(Bnd{ a, b, tw, M.h[e].cons });
+                if (tw >= 0 || orient(M, a, b, x, y) > 0) bnd.push_back(Bnd{ a, b, tw, M.h[e].cons != 0 });
             }
             e = M.h[e].next;
         } while (e != h0);
@@ -552,7 +554,7 @@ int mesh_insert_point(Context& c, double x, double y, bool)
         const int t = M.h[e].tri;
         if (t >= 0 && in_cav(t)) continue;
         const int a = M.h[e].org, b = M.h[M.h[e].next].org;
-        bnd.push_back(Bnd{ b, a, e, M.h[e].cons });
+        bnd.push_back(Bnd{ b, a, e, M.h[e].cons != 0 });
     }
 
     std::sort(cav_tri.rbegin(), cav_tri.rend());

@@ -176,3 +176,52 @@ def test_insert_into_empty_and_duplicates(lib):
             assert t.insert_point(float(x), float(y))[0] == 0
         allp = np.concatenate([[[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 0.0]], p])
         assert np.array_equal(O.canonical(t.triangles_array()), O.canonical(O.triangulate(allp).tris))
+
+
+def _ops_sequence(pts, seed):
+    """Insertions (inside, on an existing point, outside the hull, on a
+    lattice line) and constraints between existing points."""
+    rng = np.random.default_rng(seed)
+    lo, hi = pts.min(axis=0), pts.max(axis=0)
+    ops = []
+    for k in range(40):
+        r = rng.random()
+        if r < 0.5:
+            x, y = lo + (hi - lo) * rng.random(2)
+            ops.append(("insert", float(x), float(y)))
+        elif r < 0.6:
+            x, y = pts[int(rng.integers(0, len(pts)))]
+            ops.append(("insert", float(x), float(y)))
+        elif r < 0.7:
+            x, y = lo - 0.2 * (hi - lo) + 1.4 * (hi - lo) * rng.random(2)
+            ops.append(("insert", float(x), float(y)))
+        else:
+            a, b = rng.integers(0, len(pts), size=2)
+            ops.append(("constraint", int(a), int(b)))
+    return ops
+
+
+def test_mesh_built_on_gpu_equals_host(lib):
+    """The first insertion or constraint builds the half-edge mesh on the GPU
+    (k_mesh.cu) or on the host; the two meshes are the same arrays, so every
+    status and the triangle list itself (order included) must agree after a
+    sequence of operations."""
+    inputs = [W.uniform(20000, 41), W.lattice_with_duplicates(48, 0.05, 42), W.unit_circle(500, 43),
+              np.concatenate([W.uniform(3000, 44), W.uniform(3000, 44)[:500]]), W.uniform(5, 45)]
+    for i, pts in enumerate(inputs):
+        ops = _ops_sequence(pts, 500 + i)
+        results = []
+        for on_gpu in (1, 0):
+            with G.Triangulation(lib) as t:
+                assert t.set_mesh_on_gpu(on_gpu)
+                assert t.execute(pts) == 0
+                sts = []
+                for op in ops:
+                    if op[0] == "insert":
+                        sts.append(t.insert_point(op[1], op[2]))
+                    else:
+                        sts.append(t.insert_constraint(op[1], op[2]))
+                results.append((sts, t.triangles_array().copy(), t.points_size()))
+        assert results[0][0] == results[1][0], i
+        assert results[0][2] == results[1][2], i
+        assert np.array_equal(results[0][1], results[1][1]), i
