@@ -62,6 +62,31 @@ QDT_API int qdtg_device_name(char* out, size_t cap);
    context. */
 QDT_API int qdtg_set_mesh_on_gpu(qdt_t* ptr, int on_gpu);
 
+/* Batch point location (extends the reference's single-point locate_,
+   GuibasStolfiDwyer_Wrapper.cpp:423-486, which qdt_insert_point runs): for
+   each of the k points, tri[i] = the smallest index (qdt_get_triangle order)
+   of a triangle that contains it, border included, or -1 beyond the hull or
+   with no triangles; where[i] (may be NULL) = -1 outside, 0 inside a
+   triangle, 1 on an edge, 2 on a vertex. The result depends only on the
+   current triangulation and the point. The walks run on the GPU over a device
+   copy of the mesh (built with it, uploaded again after insertions or
+   constraints changed it). Checks: QDT_ERR_NULL_CONTEXT, QDT_ERR_NULL_ARGUMENT
+   (pts or tri NULL with k > 0), QDT_ERR_NOT_FINITE (any coordinate; nothing
+   is written); QDT_ERR_OUT_OF_MEMORY when the device copy cannot be made. */
+QDT_API qdt_status qdtg_locate_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k, int64_t* tri, int32_t* where);
+
+/* qdt_insert_point() for each of the k points in order, with the same
+   results (points, representatives, triangles in the same order). The
+   points are located on the GPU first, so every insertion's walk starts next
+   to its point instead of at the previous insertion. results[i] (may be NULL)
+   = each entry's status; indices[i] (may be NULL) = the new point's index, or
+   (size_t)-1 when the entry was rejected. Returns the first non-OK status,
+   or QDT_OK. A rejected point (QDT_ERR_NOT_FINITE, QDT_ERR_TOO_MANY_POINTS)
+   changes nothing; a failure that empties the context (as in
+   qdt_insert_point) stops the loop and is reported for the remaining entries. */
+QDT_API qdt_status qdtg_insert_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k, size_t* indices,
+    qdt_status* results);
+
 /* The context's build merges with a whole warp per node at the depths that
    have at most warp_nodes nodes (few merges: each one's latency counts) and
    with one thread per node below (many merges); default 4096. Returns 1, or

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
 GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_nodes", "qdtg_set_defaults",
-               "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu",
+               "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -87,6 +87,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_warp_nodes.restype = ctypes.c_int
     lib.qdtg_set_mesh_on_gpu.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_mesh_on_gpu.restype = ctypes.c_int
+    lib.qdtg_locate_points.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    lib.qdtg_locate_points.restype = ctypes.c_int
+    lib.qdtg_insert_points.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    lib.qdtg_insert_points.restype = ctypes.c_int
     lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 6
     lib.qdtg_set_defaults.restype = ctypes.c_int
     lib.qdtg_device_name.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -196,6 +200,29 @@ class Triangulation(qdt_api.Context):
 
     def set_mesh_on_gpu(self, on_gpu: bool) -> bool:
         return self.lib.qdtg_set_mesh_on_gpu(self.ptr, int(bool(on_gpu))) == 1
+
+    def locate(self, pts):
+        """(status, tri, where) for an (k, 2) array of query points: the
+        smallest index of a triangle containing each point (-1 outside) and
+        its class (-1 outside, 0 inside, 1 on an edge, 2 on a vertex)."""
+        q = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 2)
+        k = q.shape[0]
+        tri = np.full(k, -1, dtype=np.int64)
+        where = np.full(k, -1, dtype=np.int32)
+        st = self.lib.qdtg_locate_points(self.ptr, q.ctypes.data if k else None, k,
+                                         tri.ctypes.data if k else None, where.ctypes.data if k else None)
+        return st, tri, where
+
+    def insert_points(self, pts):
+        """(status, results, indices): qdt_insert_point for each row in order,
+        the points located on the GPU first."""
+        q = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 2)
+        k = q.shape[0]
+        res = np.zeros(k, dtype=np.int32)
+        idx = np.zeros(k, dtype=np.uint64)
+        st = self.lib.qdtg_insert_points(self.ptr, q.ctypes.data if k else None, k,
+                                         idx.ctypes.data if k else None, res.ctypes.data if k else None)
+        return st, res, idx
 
     def execute_device(self, d_ptr: int, n: int, stream: int = 0) -> int:
         return self.lib.qdtg_execute_device(self.ptr, d_ptr, n, stream or None)

@@ -395,6 +395,83 @@ QDT_API int qdtg_set_mesh_on_gpu(qdt_t* ptr, int on_gpu)
     return 1;
 }
 
+QDT_API qdt_status qdtg_locate_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k, int64_t* tri, int32_t* where)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    if (k == 0) return QDT_OK;
+    if (!pts || !tri) return QDT_ERR_NULL_ARGUMENT;
+    for (size_t i = 0; i < k; ++i)
+        if (!point_ok(pts[i].x, pts[i].y)) return QDT_ERR_NOT_FINITE;
+    try
+    {
+        std::vector<int> t(k), w(k);
+        const int        st = qdtg::mesh_locate(*c, &pts[0].x, k, t.data(), w.data(), nullptr);
+        if (st != QDT_OK) return (qdt_status)st;
+        for (size_t i = 0; i < k; ++i)
+        {
+            tri[i] = t[i];
+            if (where) where[i] = w[i];
+        }
+        return QDT_OK;
+    }
+    catch (...)
+    {
+        return status_from_current_exception();
+    }
+}
+
+QDT_API qdt_status qdtg_insert_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k, size_t* indices,
+    qdt_status* results)
+{
+    Context* c = ctx(ptr);
+    auto     fail_all = [&](qdt_status st) {
+        fill_results(results, k, st);
+        if (indices)
+            for (size_t i = 0; i < k; ++i) indices[i] = (size_t)-1;
+        return st;
+    };
+    if (!c) return fail_all(QDT_ERR_NULL_CONTEXT);
+    if (k == 0) return QDT_OK;
+    if (!pts) return fail_all(QDT_ERR_NULL_ARGUMENT);
+    try
+    {
+        const std::vector<int> hints = qdtg::mesh_insert_hints(*c, &pts[0].x, k);
+        qdt_status             first = QDT_OK;
+        for (size_t i = 0; i < k; ++i)
+        {
+            qdt_status st;
+            if (!point_ok(pts[i].x, pts[i].y))
+                st = QDT_ERR_NOT_FINITE;
+            else if (c->npoints() >= qdtg::kMaxPoints)
+                st = QDT_ERR_TOO_MANY_POINTS;
+            else
+            {
+                st = (qdt_status)qdtg::mesh_insert_point(*c, pts[i].x, pts[i].y, false, hints[i]);
+                if (st != QDT_OK)
+                {
+                    // as qdt_insert_point: a failed rebuild leaves the context empty
+                    c->reset();
+                    fill_results(results ? results + i : nullptr, k - i, st);
+                    if (indices)
+                        for (size_t j = i; j < k; ++j) indices[j] = (size_t)-1;
+                    return st;
+                }
+            }
+            if (results) results[i] = st;
+            if (indices) indices[i] = st == QDT_OK ? c->npoints() - 1 : (size_t)-1;
+            if (st != QDT_OK && first == QDT_OK) first = st;
+        }
+        return first;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        return fail_all(st);
+    }
+}
+
 QDT_API int qdtg_set_warp_nodes(qdt_t* ptr, int warp_nodes)
 {
     Context* c = ctx(ptr);

@@ -8,6 +8,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <memory>
+#include <vector>
 
 #include "engine.hpp"
 
@@ -46,8 +47,20 @@ int rebuild_from_points(Context& c);
 
 // mesh.cu -- incremental insertion and constrained edges on the host.
 // Both may throw std::bad_alloc; they return a qdt_status value otherwise.
-int  mesh_insert_point(Context& c, double x, double y, bool parallel_build);
+// hint: a half-edge to start the point location from (-1: the last insertion)
+int  mesh_insert_point(Context& c, double x, double y, bool parallel_build, int hint = -1);
 int  mesh_insert_constraint(Context& c, size_t v0, size_t v1);
+// Locates k points (x, y pairs, finite) in the current triangulation: per
+// point the smallest index of a triangle containing it (border included) or
+// -1, its class (mesh_walk.cuh LocClass: -1 outside, 0 inside, 1 on an edge,
+// 2 on a vertex), and, if he is not NULL, a half-edge next to it (a start
+// for the walk of a later insertion). Runs on the GPU when the context has
+// an engine; walks the device gives up on finish on the host.
+int  mesh_locate(Context& c, const double* xy, size_t k, int* tri, int* where, int* he);
+// Walk starts for inserting k points in order (-1: none): their locations in
+// the current mesh, found on the GPU when that pays. A hint only shortens the
+// walk; the insertion result does not depend on it.
+std::vector<int> mesh_insert_hints(Context& c, const double* xy, size_t k);
 void mesh_destroy(Mesh* m) noexcept;
 
 }  // namespace qdtg

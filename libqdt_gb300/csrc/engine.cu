@@ -135,7 +135,8 @@ Engine* Engine::create(int* cuda_error)
     for (auto& ev : g->ev_)
         cudaEventCreate(&ev);
     g->w_ = new (std::nothrow) DeviceWork();
-    if (!g->w_)
+    g->mirror_ = new (std::nothrow) MeshMirror();
+    if (!g->w_ || !g->mirror_)
     {
         delete g;
         return nullptr;
@@ -158,6 +159,11 @@ Engine::~Engine()
         if (w_->block) cudaFree(w_->block);
         if (w_->hsmall) cudaFreeHost(w_->hsmall);
         delete w_;
+    }
+    if (mirror_)
+    {
+        mirror_free(*mirror_);
+        delete mirror_;
     }
     for (auto& ev : ev_)
         if (ev) cudaEventDestroy(ev);
@@ -240,7 +246,14 @@ int Engine::build_mesh(size_t n, size_t T, MeshVec<int>& o2l, MeshVec<MeshVertex
         cudaGetLastError();
         return -1;
     }
-    return mesh_build_device(w_->build.tris, w_->pts, n, T, stream_, o2l, v, h);
+    return mesh_build_device(w_->build.tris, w_->pts, n, T, stream_, *mirror_, o2l, v, h);
+}
+
+bool Engine::activate()
+{
+    if (cudaSetDevice(device_) == cudaSuccess) return true;
+    cudaGetLastError();
+    return false;
 }
 
 const uint32_t* Engine::device_triangles() const { return w_ ? w_->build.tris : nullptr; }

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "mesh_layout.hpp"
+#include "mesh_mirror.hpp"
 
 namespace qdtg {
 
@@ -133,6 +134,12 @@ public:
     // then builds the mesh on the host).
     int build_mesh(size_t n, size_t T, MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h);
 
+    // The device copy of the handle's mesh for batch point location
+    // (mesh_mirror.hpp); build_mesh fills it. Calls on it run on stream().
+    MeshMirror& mirror() { return *mirror_; }
+    // makes this engine's device current; false on failure
+    bool        activate();
+
     const uint32_t* device_triangles() const;
     const uint32_t* device_rep() const;
     size_t          last_ntri() const { return info_.ntri; }
@@ -161,6 +168,7 @@ private:
     int             warp_nodes_ = 4096;
     bool            mesh_source_ = false;   // the device holds the last run_host's points and triangles
     size_t          mesh_n_ = 0, mesh_t_ = 0;
+    MeshMirror*     mirror_ = nullptr;
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "mesh_layout.hpp"
+#include "mesh_mirror.hpp"
 
 namespace qdtg {
 
@@ -70,9 +71,10 @@ void launch_split(PrepBuffers& b, int m, cudaStream_t s);
 void launch_finalize(const PrepBuffers& b, int m, cudaStream_t s);
 
 // the half-edge mesh of T triangles (3 T point indices) over n points, both on
-// the device, into host arrays (k_mesh.cu); 0 or a negative value
+// the device, into host arrays (k_mesh.cu); the vertices and half-edges stay
+// in the mirror as well. 0 or a negative value
 int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t T, cudaStream_t s,
-    MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h);
+    MeshMirror& mir, MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h);
 
 // builds every level from the deepest to the root
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s);

@@ -22,6 +22,7 @@
 #include "engine.hpp"
 #include "engine_kernels.hpp"
 #include "mesh_layout.hpp"
+#include "mesh_mirror.hpp"
 #include "scan.cuh"
 
 namespace qdtg {
@@ -116,11 +117,16 @@ inline unsigned grid(size_t n) { return (unsigned)((n + 255) / 256); }
 }  // namespace
 
 int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t T, cudaStream_t s,
-    MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h)
+    MeshMirror& mir, MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h)
 {
     if (T == 0 || 3 * T > 0x7FFFFFFFull || n > 0x7FFFFFFFull) return -1;
     const uint32_t n3 = (uint32_t)(3 * T), un = (uint32_t)n;
-    // working memory: first[n], lid[3T], o2l[n], v[n], h[3T], deg[n], off[n+1], cursor[n], adj[3T], scan scratch
+    // the vertices and half-edges are built in the mirror, which keeps them
+    // for the batch point location
+    mir.mesh_version = ~0ull;
+    mir.nv = mir.nh = 0;
+    if (mirror_reserve(mir, n, n3) != 0) return -1;
+    // working memory: first[n], lid[3T], o2l[n], deg[n], off[n+1], cursor[n], adj[3T], scan scratch
     const size_t sw = scan_scratch_words(std::max<size_t>(n3, n + 1)) + 8;
     size_t       bytes = 0;
     auto         take = [&](size_t b) {
@@ -128,10 +134,9 @@ int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t
         bytes += (b + 255) & ~(size_t)255;
         return o;
     };
-    const size_t o_first = take(n * 4), o_lid = take((size_t)n3 * 4), o_o2l = take(n * 4),
-                 o_v = take(n * sizeof(MeshVertex)), o_h = take((size_t)n3 * sizeof(MeshHalfEdge)),
-                 o_deg = take(n * 4), o_off = take((n + 1) * 4), o_cur = take(n * 4), o_adj = take((size_t)n3 * 4),
-                 o_scr = take(sw * 4), o_tot = take(16);
+    const size_t o_first = take(n * 4), o_lid = take((size_t)n3 * 4), o_o2l = take(n * 4), o_deg = take(n * 4),
+                 o_off = take((n + 1) * 4), o_cur = take(n * 4), o_adj = take((size_t)n3 * 4), o_scr = take(sw * 4),
+                 o_tot = take(16);
     char* base = nullptr;
     if (cudaMalloc(&base, bytes) != cudaSuccess)
     {
@@ -141,8 +146,8 @@ int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t
     int*          first = reinterpret_cast<int*>(base + o_first);
     uint32_t*     lid = reinterpret_cast<uint32_t*>(base + o_lid);
     int*          d_o2l = reinterpret_cast<int*>(base + o_o2l);
-    MeshVertex*   d_v = reinterpret_cast<MeshVertex*>(base + o_v);
-    MeshHalfEdge* d_h = reinterpret_cast<MeshHalfEdge*>(base + o_h);
+    MeshVertex*   d_v = mir.v;
+    MeshHalfEdge* d_h = mir.h;
     uint32_t*     deg = reinterpret_cast<uint32_t*>(base + o_deg);
     uint32_t*     off = reinterpret_cast<uint32_t*>(base + o_off);
     uint32_t*     cur = reinterpret_cast<uint32_t*>(base + o_cur);
@@ -184,6 +189,11 @@ int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t
             if (nv) cudaMemcpyAsync(v.data(), d_v, (size_t)nv * sizeof(MeshVertex), cudaMemcpyDeviceToHost, s);
             cudaMemcpyAsync(h.data(), d_h, (size_t)n3 * sizeof(MeshHalfEdge), cudaMemcpyDeviceToHost, s);
             if (cudaStreamSynchronize(s) != cudaSuccess) rc = -1;
+        }
+        if (rc == 0)
+        {
+            mir.nv = nv;
+            mir.nh = n3;
         }
     }
     cudaGetLastError();

@@ -19,12 +19,16 @@
 //
 // All geometric decisions use the exact predicates of predicates.cuh.
 #include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cmath>
 #include <deque>
 #include <unordered_map>
 #include <vector>
 
 #include "context.hpp"
 #include "mesh_layout.hpp"
+#include "mesh_walk.cuh"
 #include "predicates.cuh"
 #include "qdt.h"
 
@@ -41,6 +45,14 @@ struct Mesh
     MeshVec<int>     o2l;    // point index -> mesh vertex, -1 when none
     std::vector<int> t2h;    // triangle -> one of its half-edges
     int              last = 0;
+    uint64_t         id = next_id();   // identifies this mesh to the device mirror
+    uint64_t         version = 0;      // bumped by every call that may change the mesh
+
+    static uint64_t next_id()
+    {
+        static std::atomic<uint64_t> n{ 0 };
+        return ++n;
+    }
 };
 
 void mesh_destroy(Mesh* m) noexcept { delete m; }
@@ -130,6 +142,24 @@ bool build_mesh_on_device(Context& c, Mesh& M)
     M.last = 0;
     M.t2h.resize(T);
     for (size_t t = 0; t < T; ++t) M.t2h[t] = (int)(3 * t);
+    MeshMirror& mr = c.engine->mirror();
+    mr.mesh_id = M.id;
+    mr.mesh_version = M.version;
+    return true;
+}
+
+// Brings the engine's device mirror to the mesh's current state (an upload
+// when the host changed it since). false when there is no engine or the
+// upload failed.
+bool sync_mirror(Context& c, const Mesh& M)
+{
+    if (!c.engine || !c.engine->activate()) return false;
+    MeshMirror& mr = c.engine->mirror();
+    if (mr.mesh_id == M.id && mr.mesh_version == M.version && mr.nv == M.v.size() && mr.nh == M.h.size())
+        return true;
+    if (mirror_upload(mr, M.v.data(), M.v.size(), M.h.data(), M.h.size(), c.engine->stream()) != 0) return false;
+    mr.mesh_id = M.id;
+    mr.mesh_version = M.version;
     return true;
 }
 
@@ -202,12 +232,13 @@ void remove_tri(Context& c, Mesh& M, size_t idx)
 
 // Visibility walk (Wrapper.cpp:423-486), scan as fallback (:491-521).
 // Returns a half-edge of the triangle containing p (border included), or -1
-// with *hull set to a hull half-edge that p sees.
-int locate(const Mesh& M, size_t ntri, double px, double py, int* hull)
+// with *hull set to a hull half-edge that p sees. The walk starts at the
+// half-edge `start` when it is alive, else at the last insertion.
+int locate(const Mesh& M, size_t ntri, double px, double py, int* hull, int start = -1)
 {
     *hull = -1;
     if (M.h.empty() || ntri == 0) return -1;
-    int h = M.last;
+    int h = (start >= 0 && start < (int)M.h.size() && M.h[start].org >= 0) ? start : M.last;
     if (h < 0 || h >= (int)M.h.size() || M.h[h].org < 0)
     {
         h = 0;
@@ -432,14 +463,15 @@ int insert_by_rebuild(Context& c, double x, double y)
 
 }  // namespace
 
-int mesh_insert_point(Context& c, double x, double y, bool)
+int mesh_insert_point(Context& c, double x, double y, bool, int hint)
 {
     if (c.ntris() == 0) return insert_by_rebuild(c, x, y);
     Mesh& M = ensure_mesh(c);
     if (M.h.empty()) return insert_by_rebuild(c, x, y);
+    ++M.version;
 
-    int       hull = -1;
-    const int h_start = locate(M, c.ntris(), x, y, &hull);
+    int hull = -1;
+    int h_start = locate(M, c.ntris(), x, y, &hull, hint);
     if (h_start < 0 && hull < 0) return insert_by_rebuild(c, x, y);
     const bool outside = h_start < 0;
     if (!outside)
@@ -458,6 +490,13 @@ int mesh_insert_point(Context& c, double x, double y, bool)
             }
             e = M.h[e].next;
         } while (e != h_start);
+        // start from the canonical containing triangle (the smaller index of
+        // the two when p lies on an edge), so that the result does not depend
+        // on where the walk began
+        const LocResult cl =
+            classify(M.v.data(), M.h.data(), (int)M.v.size(), (int)M.h.size(), h_start, x, y, INT_MAX);
+        if ((cl.where == kLocInside || cl.where == kLocEdge) && cl.tri >= 0 && cl.tri < (int)M.t2h.size())
+            h_start = M.t2h[cl.tri];
     }
     M.last = outside ? hull : h_start;
 
@@ -490,9 +529,13 @@ int mesh_insert_point(Context& c, double x, double y, bool)
             }
             return k;
         };
-        visible.push_back(hull);
-        for (int e = next_hull(hull); e != hull && vis(e); e = next_hull(e)) visible.push_back(e);
-        for (int e = prev_hull(hull); e != hull && vis(e); e = prev_hull(e)) visible.push_back(e);
+        // the visible hull edges form one chain; list it from its first edge
+        // (in hull order), whichever edge the walk found
+        int s = hull;
+        for (int e = prev_hull(hull); e != hull && vis(e); e = prev_hull(e)) s = e;
+        visible.push_back(s);
+        for (int e = next_hull(s); e != s && vis(e); e = next_hull(e)) visible.push_back(e);
+        M.last = s;
     }
 
     // the cavity: the triangle that contains p, and the one across the edge p
@@ -659,7 +702,8 @@ int mesh_insert_constraint(Context& c, size_t v0, size_t v1)
     v0 = c.rep[v0];
     v1 = c.rep[v1];
     if (v0 == v1) return QDT_ERR_SAME_POINT;
-    Mesh&     M = ensure_mesh(c);
+    Mesh& M = ensure_mesh(c);
+    ++M.version;
     const int u = v0 < M.o2l.size() ? M.o2l[v0] : -1;
     const int w = v1 < M.o2l.size() ? M.o2l[v1] : -1;
     if (u < 0 || w < 0) return QDT_ERR_NO_TRIANGLES;
@@ -735,6 +779,89 @@ int mesh_insert_constraint(Context& c, size_t v0, size_t v1)
     for (int h : queue) around(h);
     legalize(c, M, stack);
     return ok ? QDT_OK : QDT_ERR_INTERNAL;
+}
+
+int mesh_locate(Context& c, const double* xy, size_t k, int* tri, int* where, int* he)
+{
+    if (k == 0) return QDT_OK;
+    auto none = [&](size_t i) {
+        tri[i] = -1;
+        where[i] = kLocOutside;
+        if (he) he[i] = -1;
+    };
+    if (c.ntris() == 0)
+    {
+        for (size_t i = 0; i < k; ++i) none(i);
+        return QDT_OK;
+    }
+    Mesh& M = ensure_mesh(c);
+    if (M.h.empty() || M.h.size() > (size_t)INT_MAX || M.v.size() > (size_t)INT_MAX)
+    {
+        for (size_t i = 0; i < k; ++i) none(i);
+        return QDT_OK;
+    }
+    std::vector<int> hev;
+    int*             hp = he;
+    if (!hp)
+    {
+        hev.resize(k);
+        hp = hev.data();
+    }
+    if (!sync_mirror(c, M)) return QDT_ERR_OUT_OF_MEMORY;
+    if (mirror_locate(c.engine->mirror(), xy, k, tri, where, hp, c.engine->stream()) != 0)
+        return QDT_ERR_OUT_OF_MEMORY;
+    // the walks the device gave up on, on the host
+    const int nv = (int)M.v.size(), nh = (int)M.h.size();
+    for (size_t i = 0; i < k; ++i)
+    {
+        if (where[i] != kLocUnresolved) continue;
+        int       hull = -1;
+        const int h0 = locate(M, c.ntris(), xy[2 * i], xy[2 * i + 1], &hull);
+        if (h0 >= 0)
+        {
+            const LocResult r = classify(M.v.data(), M.h.data(), nv, nh, h0, xy[2 * i], xy[2 * i + 1], INT_MAX);
+            tri[i] = r.tri;
+            where[i] = r.where;
+            hp[i] = h0;
+        }
+        else
+        {
+            tri[i] = -1;
+            where[i] = kLocOutside;
+            hp[i] = hull;
+        }
+    }
+    return QDT_OK;
+}
+
+std::vector<int> mesh_insert_hints(Context& c, const double* xy, size_t k)
+{
+    std::vector<int> hints(k, -1);
+    if (k < 2 || c.ntris() == 0 || !c.engine) return hints;
+    Mesh& M = ensure_mesh(c);
+    if (M.h.empty() || M.h.size() > (size_t)INT_MAX) return hints;
+    // Without hints each walk crosses about sqrt(half-edges) triangles; a
+    // stale mirror costs an upload of the whole mesh. Locate on the device
+    // when the mirror is current, or when the walks saved outweigh the upload.
+    const MeshMirror& mr = c.engine->mirror();
+    const bool current = mr.mesh_id == M.id && mr.mesh_version == M.version && mr.nh == M.h.size();
+    if (!current && (double)k < std::sqrt((double)M.h.size()) / 8.0) return hints;
+    std::vector<double> q;
+    std::vector<size_t> at;
+    q.reserve(2 * k);
+    at.reserve(k);
+    for (size_t i = 0; i < k; ++i)
+        if (std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]))
+        {
+            q.push_back(xy[2 * i]);
+            q.push_back(xy[2 * i + 1]);
+            at.push_back(i);
+        }
+    const size_t     m = at.size();
+    std::vector<int> tri(m), where(m), he(m);
+    if (m == 0 || mesh_locate(c, q.data(), m, tri.data(), where.data(), he.data()) != QDT_OK) return hints;
+    for (size_t j = 0; j < m; ++j) hints[at[j]] = he[j];
+    return hints;
 }
 
 }  // namespace qdtg

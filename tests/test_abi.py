@@ -141,3 +141,23 @@ def test_batch_and_server_host_checks(lib):
     assert not lib.qdtg_server_create(ctypes.byref(bad))
     assert lib.qdtg_server_wait(None, 1, 0.0) == -1
     assert lib.qdtg_server_release(None, 1) == 0
+
+
+def test_locate_and_batch_insert_host_checks(lib):
+    """Batch location and batch insertion: argument checks, NaN queries, and
+    the context without triangles (every point outside), none of which needs
+    the GPU."""
+    assert lib.qdtg_locate_points(None, None, 0, None, None) == Q.QDT_ERR_NULL_CONTEXT
+    res = np.zeros(3, dtype=np.int32)
+    idx = np.zeros(3, dtype=np.uint64)
+    assert lib.qdtg_insert_points(None, None, 3, idx.ctypes.data, res.ctypes.data) == Q.QDT_ERR_NULL_CONTEXT
+    assert (res == Q.QDT_ERR_NULL_CONTEXT).all() and (idx == np.iinfo(np.uint64).max).all()
+    with G.Triangulation(lib) as t:
+        assert lib.qdtg_locate_points(t.ptr, None, 2, None, None) == Q.QDT_ERR_NULL_ARGUMENT
+        assert lib.qdtg_insert_points(t.ptr, None, 2, None, None) == Q.QDT_ERR_NULL_ARGUMENT
+        assert lib.qdtg_insert_points(t.ptr, None, 0, None, None) == Q.QDT_OK
+        st, tri, where = t.locate(np.array([[0.5, 0.5], [np.inf, 0.0]]))
+        assert st == Q.QDT_ERR_NOT_FINITE and (tri == -1).all()
+        st, tri, where = t.locate(np.array([[0.5, 0.5], [3.0, -1.0]]))
+        assert st == Q.QDT_OK and (tri == -1).all() and (where == -1).all()
+        assert t.points_size() == 0
