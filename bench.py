@@ -330,6 +330,8 @@ def run_gb300(args):
             line["batched"] = run_batched_leg(lib, args, flush)
         if "serving" in legs:
             line["serving"] = run_serving_leg(lib, args)
+        if "handle" in legs:
+            line["handle"] = run_handle_leg(lib, pts, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -451,6 +453,74 @@ def run_serving_leg(lib, args):
     return out
 
 
+def run_handle_leg(lib, pts, args):
+    """Handle operations after a batch call on the workload's points: the
+    first insertion (the half-edge mesh built on the GPU from the resident
+    result), batch location of 1,000,000 random points (qdtg_locate_points),
+    and 20,000 random insertions through qdtg_insert_points against
+    qdt_insert_point called point by point (2,000 points; per-point cost
+    compared). Wall clock through the C ABI with host buffers."""
+    import numpy as np
+
+    import libqdt_gb300 as G
+
+    rng = np.random.default_rng(31)
+    lo, hi = pts.min(0), pts.max(0)
+    q = lo + rng.random((1_000_000, 2)) * (hi - lo)
+    ins = lo + rng.random((20_000, 2)) * (hi - lo)
+    seq = lo + rng.random((2_000, 2)) * (hi - lo)
+    out = {"workload": "the bench points; 1e6 random queries, 2e4 batch + 2e3 single insertions (seed 31)"}
+    with G.Triangulation(lib) as t:
+        ms = []
+        for _ in range(3):
+            t.execute(pts)
+            a = time.perf_counter()
+            st, _ = t.insert_point(float(ins[0, 0]), float(ins[0, 1]))
+            ms.append(1e3 * (time.perf_counter() - a))
+            if st != 0:
+                raise RuntimeError("qdt_insert_point failed: %d" % st)
+        out["first_insert_ms"] = round(statistics.median(ms), 2)
+        t.execute(pts)
+        a = time.perf_counter()
+        st, _, _ = t.locate(q[:1])
+        out["mesh_build_and_index_ms"] = round(1e3 * (time.perf_counter() - a), 2)
+        ms = []
+        for _ in range(3):
+            a = time.perf_counter()
+            st, tri, where = t.locate(q)
+            ms.append(1e3 * (time.perf_counter() - a))
+            if st != 0:
+                raise RuntimeError("qdtg_locate_points failed: %d" % st)
+        out["locate_1e6_ms"] = round(statistics.median(ms), 2)
+        out["locate_mqueries_per_s"] = round(1.0 / statistics.median(ms) * 1e3, 2)
+        out["outside"] = int((where < 0).sum())
+        a = time.perf_counter()
+        st, res, _ = t.insert_points(ins)
+        b = time.perf_counter()
+        if st != 0:
+            raise RuntimeError("qdtg_insert_points failed: %d" % st)
+        out["insert_points_us_per_point"] = round(1e6 * (b - a) / len(ins), 3)
+        a = time.perf_counter()
+        for x, y in seq:
+            t.insert_point(float(x), float(y))
+        b = time.perf_counter()
+        out["insert_point_us_per_point"] = round(1e6 * (b - a) / len(seq), 3)
+        out["speedup_batch_insert"] = round(out["insert_point_us_per_point"] / out["insert_points_us_per_point"], 2)
+        a = time.perf_counter()
+        t.locate(q)
+        out["locate_1e6_after_edits_ms"] = round(1e3 * (time.perf_counter() - a), 2)
+        # constraint tracing: 10,000 segments between random points (long:
+        # each crosses on the order of sqrt(n) edges)
+        segs = rng.integers(0, pts.shape[0], size=(10_000, 2))
+        t.trace_constraints(segs[:10])
+        a = time.perf_counter()
+        st, status, crossed = t.trace_constraints(segs)
+        out["trace_1e4_ms"] = round(1e3 * (time.perf_counter() - a), 2)
+        out["trace_mean_crossed"] = round(float(crossed.mean()), 1)
+        out["trace_ok"] = int((status == 0).sum())
+    return out
+
+
 def run_profile_target(args):
     """Runs one form of the path (warmup + steps calls, device-resident input,
     no timing, no L2 flush, no checks) for a profiler to capture: 'single'
@@ -496,8 +566,8 @@ def main():
     ap.add_argument("--workload", default="uniform_2p6m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--legs", default="batched,serving",
-                    help="extra legs in the same line (rank 0, one GPU): batched, serving; '' for none")
+    ap.add_argument("--legs", default="batched,serving,handle",
+                    help="extra legs in the same line (rank 0, one GPU): batched, serving, handle; '' for none")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner's choice")
     ap.add_argument("--profile-run", choices=["single", "batched"],

@@ -87,6 +87,23 @@ QDT_API qdt_status qdtg_locate_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k
 QDT_API qdt_status qdtg_insert_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k, size_t* indices,
     qdt_status* results);
 
+/* Constraint tracing for a validation pass (the reference's trace_segment_,
+   GuibasStolfiDwyer_Wrapper.cpp:1050-1106, and the checks before it,
+   :1158-1165 and :1246-1261): for each of the k edges, on its
+   own against the current triangulation (nothing is inserted), status[i] =
+   what qdt_insert_constraint() would return for it as the next call
+   (QDT_OK, QDT_ERR_INVALID_INDEX, QDT_ERR_SAME_POINT, QDT_ERR_NO_TRIANGLES,
+   QDT_ERR_THROUGH_POINT, QDT_ERR_CROSSES_CONSTRAINT) and crossed[i] (may be
+   NULL) = the number of edges its segment crosses before that decision (0
+   when the edge exists; for QDT_OK, the edges the insertion flips away).
+   Entries do not see each other: use qdt_insert_constraints_batch() to apply
+   them in order. The traces run on the GPU over the device copy of the mesh
+   (see qdtg_locate_points). Returns QDT_ERR_NULL_CONTEXT,
+   QDT_ERR_NULL_ARGUMENT (edges or status NULL with k > 0),
+   QDT_ERR_OUT_OF_MEMORY, or QDT_OK. */
+QDT_API qdt_status qdtg_trace_constraints(qdt_t* ptr, const qdt_edge* edges, size_t k, qdt_status* status,
+    int64_t* crossed);
+
 /* The context's build merges with a whole warp per node at the depths that
    have at most warp_nodes nodes (few merges: each one's latency counts) and
    with one thread per node below (many merges); default 4096. Returns 1, or

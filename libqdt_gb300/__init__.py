@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
 GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_nodes", "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
+               "qdtg_trace_constraints",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -91,6 +92,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_locate_points.restype = ctypes.c_int
     lib.qdtg_insert_points.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
     lib.qdtg_insert_points.restype = ctypes.c_int
+    lib.qdtg_trace_constraints.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    lib.qdtg_trace_constraints.restype = ctypes.c_int
     lib.qdtg_set_defaults.argtypes = [ctypes.c_int] * 6
     lib.qdtg_set_defaults.restype = ctypes.c_int
     lib.qdtg_device_name.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -223,6 +226,18 @@ class Triangulation(qdt_api.Context):
         st = self.lib.qdtg_insert_points(self.ptr, q.ctypes.data if k else None, k,
                                          idx.ctypes.data if k else None, res.ctypes.data if k else None)
         return st, res, idx
+
+    def trace_constraints(self, edges):
+        """(status, per-edge statuses, crossed): what qdt_insert_constraint
+        would return for each edge on its own now, and the edges its segment
+        crosses; nothing is inserted."""
+        e = np.ascontiguousarray(edges, dtype=np.uint64).reshape(-1, 2)
+        k = e.shape[0]
+        res = np.zeros(k, dtype=np.int32)
+        crossed = np.zeros(k, dtype=np.int64)
+        st = self.lib.qdtg_trace_constraints(self.ptr, e.ctypes.data if k else None, k,
+                                             res.ctypes.data if k else None, crossed.ctypes.data if k else None)
+        return st, res, crossed
 
     def execute_device(self, d_ptr: int, n: int, stream: int = 0) -> int:
         return self.lib.qdtg_execute_device(self.ptr, d_ptr, n, stream or None)

@@ -421,6 +421,33 @@ QDT_API qdt_status qdtg_locate_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k
     }
 }
 
+QDT_API qdt_status qdtg_trace_constraints(qdt_t* ptr, const qdt_edge* edges, size_t k, qdt_status* status,
+    int64_t* crossed)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    if (k == 0) return QDT_OK;
+    if (!edges || !status) return QDT_ERR_NULL_ARGUMENT;
+    static_assert(sizeof(qdt_edge) == 2 * sizeof(size_t), "qdt_edge is two size_t");
+    try
+    {
+        std::vector<int>     st(k);
+        std::vector<int64_t> cr(k);
+        const int            rc = qdtg::mesh_trace_segments(*c, &edges[0].v0, k, st.data(), cr.data());
+        if (rc != QDT_OK) return (qdt_status)rc;
+        for (size_t i = 0; i < k; ++i)
+        {
+            status[i] = (qdt_status)st[i];
+            if (crossed) crossed[i] = cr[i];
+        }
+        return QDT_OK;
+    }
+    catch (...)
+    {
+        return status_from_current_exception();
+    }
+}
+
 QDT_API qdt_status qdtg_insert_points(qdt_t* ptr, const qdt_vec2d* pts, size_t k, size_t* indices,
     qdt_status* results)
 {

@@ -61,6 +61,12 @@ int  mesh_locate(Context& c, const double* xy, size_t k, int* tri, int* where, i
 // the current mesh, found on the GPU when that pays. A hint only shortens the
 // walk; the insertion result does not depend on it.
 std::vector<int> mesh_insert_hints(Context& c, const double* xy, size_t k);
+// For k constraints (v0, v1 pairs), each on its own against the current
+// triangulation: the status mesh_insert_constraint would return for it as
+// the next call, and the number of edges its segment crosses before the
+// decision (the edges the insertion would flip when it is accepted). The
+// traces run on the GPU. Returns QDT_OK or the status of a device failure.
+int mesh_trace_segments(Context& c, const size_t* v01, size_t k, int* status, int64_t* crossed);
 void mesh_destroy(Mesh* m) noexcept;
 
 }  // namespace qdtg

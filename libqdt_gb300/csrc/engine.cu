@@ -352,6 +352,11 @@ int Engine::run_host(const double* xy, size_t n, PinnedVec<double>& points, Pinn
     if (st != S_OK) return st;
     // host copies the caller's points into the context (pinned) in chunks; the
     // upload of a chunk overlaps the copy of the next one
+    // room for later insertions: growing a page-locked vector reallocates
+    // and re-pins it
+    const size_t room = n + std::max<size_t>(n / 16, 1024);
+    if (points.capacity() < 2 * n) points.reserve(2 * room);
+    if (rep.capacity() < n) rep.reserve(room);
     points.resize(2 * n);
     rep.resize(n);
     tris.resize(6 * n + 3);

@@ -120,6 +120,19 @@ __global__ void k_mesh_locate(const MeshVertex* __restrict__ v, const MeshHalfEd
     out[i] = make_int4(r.tri, r.where, r.he, 0);
 }
 
+// one thread per constraint segment (mesh vertices u, w): the trace outcome
+// and the edges crossed
+__global__ void k_mesh_trace(const MeshVertex* __restrict__ v, const MeshHalfEdge* __restrict__ h, int nv, int nh,
+    const int2* __restrict__ uw, size_t k, int2* __restrict__ out)
+{
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    const int2 s = uw[i];
+    int        crossed = 0;
+    const int  r = trace_segment(v, h, nv, nh, s.x, s.y, kWalkCap, &crossed);
+    out[i] = make_int2(r, crossed);
+}
+
 inline unsigned blocks(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 template <class T>
@@ -221,11 +234,9 @@ int mirror_upload(MeshMirror& m, const MeshVertex* v, size_t nv, const MeshHalfE
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int mirror_locate(MeshMirror& m, const double* xy, size_t k, int* tri, int* where, int* he, cudaStream_t s)
+// k query slots: 16 bytes in (q) and 16 bytes out (out) each
+static int query_buffers(MeshMirror& m, size_t k)
 {
-    if (k == 0) return 0;
-    if (m.nv > 0x7FFFFFFFull || m.nh > 0x7FFFFFFFull) return -1;
-    if (!m.indexed && build_index(m, s) != 0) return -1;
     if (k > m.cap_q || !m.q || !m.out)
     {
         if (m.q) cudaFree(m.q);
@@ -245,6 +256,15 @@ int mirror_locate(MeshMirror& m, const double* xy, size_t k, int* tri, int* wher
         }
         m.cap_q = want;
     }
+    return 0;
+}
+
+int mirror_locate(MeshMirror& m, const double* xy, size_t k, int* tri, int* where, int* he, cudaStream_t s)
+{
+    if (k == 0) return 0;
+    if (m.nv > 0x7FFFFFFFull || m.nh > 0x7FFFFFFFull) return -1;
+    if (!m.indexed && build_index(m, s) != 0) return -1;
+    if (query_buffers(m, k) != 0) return -1;
     std::vector<int4> res(k);
     cudaMemcpyAsync(m.q, xy, k * sizeof(double2), cudaMemcpyHostToDevice, s);
     const Grid g{ m.gx, m.gy, m.x0, m.y0, m.ix, m.iy };
@@ -257,6 +277,27 @@ int mirror_locate(MeshMirror& m, const double* xy, size_t k, int* tri, int* wher
         tri[i] = res[i].x;
         where[i] = res[i].y;
         he[i] = res[i].z;
+    }
+    return 0;
+}
+
+int mirror_trace(MeshMirror& m, const int* uw, size_t k, int* outcome, int* crossed, cudaStream_t s)
+{
+    if (k == 0) return 0;
+    if (m.nv > 0x7FFFFFFFull || m.nh > 0x7FFFFFFFull) return -1;
+    if (query_buffers(m, k) != 0) return -1;
+    std::vector<int2> res(k);
+    int2*             d_uw = reinterpret_cast<int2*>(m.q);     // 8 of the slot's 16 bytes
+    int2*             d_out = reinterpret_cast<int2*>(m.out);
+    cudaMemcpyAsync(d_uw, uw, k * sizeof(int2), cudaMemcpyHostToDevice, s);
+    k_mesh_trace<<<blocks(k, 128), 128, 0, s>>>(m.v, m.h, (int)m.nv, (int)m.nh, d_uw, k, d_out);
+    ++launch_counter();
+    cudaMemcpyAsync(res.data(), d_out, k * sizeof(int2), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    for (size_t i = 0; i < k; ++i)
+    {
+        outcome[i] = res[i].x;
+        crossed[i] = res[i].y;
     }
     return 0;
 }

@@ -175,6 +175,12 @@ int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t
         k_mesh_twins<<<grid(n3), 256, 0, s>>>(d_h, n3, off, deg, nv, adj);
         try
         {
+            // capacity for later insertions (untouched pages cost nothing):
+            // growing would copy the whole array
+            auto room = [](size_t s) { return s + std::max<size_t>(s / 8, 1024); };
+            o2l.reserve(room(n));
+            v.reserve(room(nv));
+            h.reserve(room(n3));
             o2l.resize(n);
             v.resize(nv);
             h.resize(n3);

@@ -140,6 +140,7 @@ bool build_mesh_on_device(Context& c, Mesh& M)
     if (c.engine->build_mesh(c.npoints(), T, M.o2l, M.v, M.h) != 0) return false;
     M.free_h.clear();
     M.last = 0;
+    M.t2h.reserve(T + std::max<size_t>(T / 8, 1024));
     M.t2h.resize(T);
     for (size_t t = 0; t < T; ++t) M.t2h[t] = (int)(3 * t);
     MeshMirror& mr = c.engine->mirror();
@@ -373,14 +374,6 @@ void mark_cons(Mesh& M, int h)
 {
     M.h[h].cons = true;
     if (M.h[h].twin >= 0) M.h[M.h[h].twin].cons = true;
-}
-
-bool same_direction(const MV& a, const MV& b, const MV& c)
-{
-    auto sg = [](double d) { return d > 0 ? 1 : (d < 0 ? -1 : 0); };
-    const int sx = sg(b.x - a.x) * sg(c.x - a.x);
-    const int sy = sg(b.y - a.y) * sg(c.y - a.y);
-    return sx >= 0 && sy >= 0 && (sx > 0 || sy > 0);
 }
 
 bool segments_cross(const Mesh& M, int a, int b, int c, int d)
@@ -830,6 +823,65 @@ int mesh_locate(Context& c, const double* xy, size_t k, int* tri, int* where, in
             where[i] = kLocOutside;
             hp[i] = hull;
         }
+    }
+    return QDT_OK;
+}
+
+int mesh_trace_segments(Context& c, const size_t* v01, size_t k, int* status, int64_t* crossed)
+{
+    if (k == 0) return QDT_OK;
+    // the checks of mesh_insert_constraint, in its order
+    std::vector<int>    uw;
+    std::vector<size_t> at;
+    Mesh*               M = nullptr;
+    for (size_t i = 0; i < k; ++i)
+    {
+        size_t v0 = v01[2 * i], v1 = v01[2 * i + 1];
+        crossed[i] = 0;
+        if (v0 >= c.rep.size() || v1 >= c.rep.size())
+        {
+            status[i] = QDT_ERR_INVALID_INDEX;
+            continue;
+        }
+        v0 = c.rep[v0];
+        v1 = c.rep[v1];
+        if (v0 == v1)
+        {
+            status[i] = QDT_ERR_SAME_POINT;
+            continue;
+        }
+        if (c.ntris() == 0)
+        {
+            status[i] = QDT_ERR_NO_TRIANGLES;
+            continue;
+        }
+        if (!M) M = &ensure_mesh(c);
+        const int u = v0 < M->o2l.size() ? M->o2l[v0] : -1;
+        const int w = v1 < M->o2l.size() ? M->o2l[v1] : -1;
+        if (u < 0 || w < 0)
+        {
+            status[i] = QDT_ERR_NO_TRIANGLES;
+            continue;
+        }
+        uw.push_back(u);
+        uw.push_back(w);
+        at.push_back(i);
+    }
+    const size_t m = at.size();
+    if (m == 0) return QDT_OK;
+    if (M->h.size() > (size_t)INT_MAX || M->v.size() > (size_t)INT_MAX) return QDT_ERR_INTERNAL;
+    std::vector<int> out(m), cr(m);
+    if (!sync_mirror(c, *M)) return QDT_ERR_OUT_OF_MEMORY;
+    if (mirror_trace(c.engine->mirror(), uw.data(), m, out.data(), cr.data(), c.engine->stream()) != 0)
+        return QDT_ERR_OUT_OF_MEMORY;
+    const int nv = (int)M->v.size(), nh = (int)M->h.size();
+    for (size_t j = 0; j < m; ++j)
+    {
+        if (out[j] == kTraceUnresolved)
+            out[j] = trace_segment(M->v.data(), M->h.data(), nv, nh, uw[2 * j], uw[2 * j + 1], INT_MAX, &cr[j]);
+        static const int map[4] = { QDT_OK, QDT_ERR_THROUGH_POINT, QDT_ERR_CROSSES_CONSTRAINT, QDT_ERR_INTERNAL };
+        status[at[j]] = (out[j] >= 0 && out[j] < 4) ? map[out[j]] : QDT_ERR_INTERNAL;
+        crossed[at[j]] = cr[j];
     }
     return QDT_OK;
 }

@@ -41,5 +41,10 @@ int  mirror_upload(MeshMirror& m, const MeshVertex* v, size_t nv, const MeshHalf
 // ended on. Points the device walk gives up on come back as kLocUnresolved.
 // 0 or -1.
 int  mirror_locate(MeshMirror& m, const double* xy, size_t k, int* tri, int* where, int* he, cudaStream_t s);
+// Traces k constraint segments (mesh vertex pairs u, w; u != w) through the
+// mirrored mesh: per segment the TraceClass (mesh_walk.cuh) and the edges
+// crossed. Segments the device gives up on come back as kTraceUnresolved.
+// 0 or -1.
+int  mirror_trace(MeshMirror& m, const int* uw, size_t k, int* outcome, int* crossed, cudaStream_t s);
 
 }  // namespace qdtg

@@ -177,4 +177,138 @@ QDT_HD inline LocResult classify(const MeshVertex* v, const MeshHalfEdge* h, int
     return r;
 }
 
+// Outcome of tracing a constraint segment through the mesh: what
+// qdt_insert_constraint decides for it before any flip
+// (GuibasStolfiDwyer_Wrapper.cpp:1050-1106 and the existing-edge check
+// before it).
+enum TraceClass : int
+{
+    kTraceOk = 0,                 // the edge exists, or the segment crosses only unconstrained edges
+    kTraceThroughPoint = 1,       // a vertex lies on the open segment
+    kTraceCrossesConstraint = 2,  // a constrained edge crosses it first
+    kTraceBroken = 3,             // the mesh around the start vertex is inconsistent
+    kTraceUnresolved = 4,         // the step limit ran out
+};
+
+QDT_HD inline bool same_direction(const MeshVertex& a, const MeshVertex& b, const MeshVertex& c)
+{
+    auto      sg = [](double d) { return d > 0 ? 1 : (d < 0 ? -1 : 0); };
+    const int sx = sg(b.x - a.x) * sg(c.x - a.x);
+    const int sy = sg(b.y - a.y) * sg(c.y - a.y);
+    return sx >= 0 && sy >= 0 && (sx > 0 || sy > 0);
+}
+
+QDT_HD inline int orient_v(const MeshVertex* v, int a, int b, int c)
+{
+    return orient2d_sign(v[a].x, v[a].y, v[b].x, v[b].y, v[c].x, v[c].y);
+}
+
+// Traces the segment from mesh vertex u to mesh vertex w (u != w). Visits
+// u's fan in the order of the host's for_each_out (counter-clockwise from
+// u's stored half-edge, then clockwise for a hull vertex): an edge u-w in
+// either direction means kTraceOk with nothing crossed; otherwise the first
+// fan triangle the segment leaves through, or a neighbour on the segment,
+// decides the start, and the march counts the edges crossed until w, a
+// vertex on the segment, or a constrained edge. *crossed = edges crossed
+// before the outcome. Each fan visit and each crossing is one step of cap.
+QDT_HD inline int trace_segment(const MeshVertex* v, const MeshHalfEdge* h, int nv, int nh, int u, int w, int cap,
+    int* crossed)
+{
+    *crossed = 0;
+    if (u < 0 || u >= nv || w < 0 || w >= nv) return kTraceBroken;
+    const int h0 = v[u].he;
+    if (!he_ok(h, nh, nv, h0) || h[h0].org != u) return kTraceBroken;
+    int  steps = 0;
+    int  start = -1;
+    bool blocked = false, exists = false;
+    // one fan visit: the existing-edge check over the whole fan, and the
+    // first start / blocking neighbour in fan order
+    auto visit = [&](int e) -> bool {
+        const int hn = h[e].next;
+        if (!he_ok(h, nh, nv, hn) || !he_ok(h, nh, nv, h[hn].next)) return false;
+        const int y = h[hn].org, z = h[h[hn].next].org;
+        if (y == w || z == w)
+        {
+            exists = true;
+            return false;
+        }
+        if (start < 0 && !blocked)
+        {
+            const int oy = orient_v(v, u, y, w), oz = orient_v(v, u, z, w);
+            if (oy > 0 && oz < 0)
+                start = hn;
+            else if ((oy == 0 && same_direction(v[u], v[y], v[w])) || (oz == 0 && same_direction(v[u], v[z], v[w])))
+                blocked = true;
+        }
+        return true;
+    };
+    bool ok = true, closed = false;
+    int  e = h0;
+    for (;;)
+    {
+        if (++steps > cap) return kTraceUnresolved;
+        if (!visit(e))
+        {
+            ok = exists;
+            break;
+        }
+        const int prev = h[h[e].next].next;
+        const int tw = h[prev].twin;
+        if (tw < 0) break;
+        if (tw == h0)
+        {
+            closed = true;
+            break;
+        }
+        if (!he_ok(h, nh, nv, tw))
+        {
+            ok = false;
+            break;
+        }
+        e = tw;
+    }
+    if (exists) return kTraceOk;
+    if (!ok) return kTraceBroken;
+    if (!closed)
+    {
+        e = h0;
+        for (;;)
+        {
+            const int tw = h[e].twin;
+            if (tw < 0) break;
+            if (!he_ok(h, nh, nv, tw)) return kTraceBroken;
+            e = h[tw].next;
+            if (e == h0) break;
+            if (!he_ok(h, nh, nv, e)) return kTraceBroken;
+            if (++steps > cap) return kTraceUnresolved;
+            if (!visit(e))
+            {
+                if (exists) return kTraceOk;
+                return kTraceBroken;
+            }
+        }
+    }
+    if (exists) return kTraceOk;
+    if (blocked) return kTraceThroughPoint;
+    if (start < 0) return kTraceBroken;
+    e = start;
+    for (;;)
+    {
+        if (++steps > cap) return kTraceUnresolved;
+        if (h[e].cons) return kTraceCrossesConstraint;
+        ++*crossed;
+        const int tw = h[e].twin;
+        if (!he_ok(h, nh, nv, tw)) return kTraceBroken;
+        const int a = h[tw].next;
+        if (!he_ok(h, nh, nv, a)) return kTraceBroken;
+        const int b = h[a].next;
+        if (!he_ok(h, nh, nv, b)) return kTraceBroken;
+        const int x = h[b].org;
+        if (x == w) return kTraceOk;
+        const int o = orient_v(v, u, w, x);
+        if (o == 0) return kTraceThroughPoint;
+        e = o > 0 ? a : b;
+    }
+}
+
 }  // namespace qdtg

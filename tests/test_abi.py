@@ -161,3 +161,7 @@ def test_locate_and_batch_insert_host_checks(lib):
         st, tri, where = t.locate(np.array([[0.5, 0.5], [3.0, -1.0]]))
         assert st == Q.QDT_OK and (tri == -1).all() and (where == -1).all()
         assert t.points_size() == 0
+        assert lib.qdtg_trace_constraints(None, None, 0, None, None) == Q.QDT_ERR_NULL_CONTEXT
+        assert lib.qdtg_trace_constraints(t.ptr, None, 1, None, None) == Q.QDT_ERR_NULL_ARGUMENT
+        st, s, c = t.trace_constraints(np.array([[0, 1], [2, 2]]))
+        assert st == Q.QDT_OK and (s == Q.QDT_ERR_INVALID_INDEX).all() and (c == 0).all()
