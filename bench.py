@@ -50,6 +50,8 @@ WORKLOADS = {
     "lattice_1024_dups": ("lattice", 1024, 7),
     "gauss_4m": ("gauss", 4000000, 11),
     "uniform_100k": ("uniform", 100000, 12345),
+    "circle_100k": ("circle", 100000, 13),
+    "line_1m": ("line", 1000000, 17),
 }
 
 
@@ -62,6 +64,10 @@ def make_points(name):
         return W.lattice_with_duplicates(n, 0.01, seed)
     if kind == "gauss":
         return W.gaussian_mixture(n, 64, seed)
+    if kind == "circle":
+        return W.unit_circle(n, seed)
+    if kind == "line":
+        return W.noisy_line(n, seed)
     raise ValueError(name)
 
 
@@ -332,6 +338,8 @@ def run_gb300(args):
             line["serving"] = run_serving_leg(lib, args)
         if "handle" in legs:
             line["handle"] = run_handle_leg(lib, pts, args)
+        if "stress" in legs:
+            line["stress"] = run_stress_leg(lib, args, flush)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -453,6 +461,82 @@ def run_serving_leg(lib, args):
     return out
 
 
+STRESS = ("uniform_1m", "lattice_1024_dups", "gauss_4m", "circle_100k", "line_1m")
+
+
+def run_stress_leg(lib, args, flush):
+    """The single-set path on the degenerate and skewed distributions:
+    1,048,576 uniform; the 1024^2 lattice with 1% exact duplicates; 4,000,000
+    points from 64 Gaussians; 100,000 points on the unit circle; 1,000,000
+    points on a line with 2^-40 noise. Per workload: device-resident
+    Mpoints/s (CUDA events on the engine's stream, L2 flushed between steps),
+    violations under the exact checker, and the predicate evaluations that
+    took the exact path on the device (counted in a separate run, per 1,000
+    points), beside the reference algorithm's filter-failure rate per call
+    (the oracle's serial builder, which restates it)."""
+    import numpy as np
+    import torch
+
+    import libqdt_gb300 as G
+    from oracle import delaunay_check as D
+    from oracle import oracle as O
+
+    out = []
+    for name in STRESS:
+        pts = make_points(name)
+        n = pts.shape[0]
+        d_pts = torch.from_numpy(pts).cuda()
+        t = G.Triangulation(lib)
+        stream = torch.cuda.ExternalStream(t.stream())
+        for _ in range(2):
+            t.execute_device(d_pts.data_ptr(), n)
+        ms = []
+        for _ in range(max(1, min(args.steps, 5))):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = t.execute_device(d_pts.data_ptr(), n)
+            e1.record(stream)
+            e1.synchronize()
+            if st != 0:
+                raise RuntimeError("%s: qdtg_execute_device failed: %d" % (name, st))
+            ms.append(e0.elapsed_time(e1))
+        t.set_options(count_filter_failures=True)
+        t.execute_device(d_pts.data_ptr(), n)
+        info = t.run_info()
+        t.set_options(count_filter_failures=False)
+        tris = t.download_device_triangles()
+        row = {"workload": name, "points": n, "distinct": info["unique_points"], "triangles": int(tris.shape[0]),
+               "value": round(n / (statistics.median(ms) / 1e3) / 1e6, 3), "unit": UNIT,
+               "ms_per_step": round(statistics.median(ms), 3),
+               "exact_per_1000_points": {"orient2d": round(1e3 * info["orient_exact"] / n, 4),
+                                         "incircle": round(1e3 * info["incircle_exact"] / n, 4)}}
+        if not args.no_check:
+            ref = O.triangulate(pts)
+            s = ref.stats
+            nt = os.cpu_count() or 1
+            a = time.perf_counter()
+            O.triangulate(pts, threaded=True, nthreads=nt)
+            cpu_s = time.perf_counter() - a
+            row["cpu_port_threaded"] = {"value": round(n / cpu_s / 1e6, 3), "unit": UNIT, "cores": nt,
+                                        "ms": round(1e3 * cpu_s, 1)}
+            res = D.check(pts, tris, ref.rep)
+            row["exact_violations"] = int(sum(res.values()))
+            row["same_triangle_count_as_oracle"] = bool(ref.tris.shape[0] == tris.shape[0])
+            row["reference_filter_failure_rate"] = {
+                "orient2d": round(s["orient_exact"] / max(1, s["orient_calls"]), 6),
+                "incircle": round(s["incircle_exact"] / max(1, s["incircle_calls"]), 6),
+                "exact_per_1000_points": {"orient2d": round(1e3 * s["orient_exact"] / n, 4),
+                                          "incircle": round(1e3 * s["incircle_exact"] / n, 4)}}
+        out.append(row)
+        t.close()
+        del d_pts
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_handle_leg(lib, pts, args):
     """Handle operations after a batch call on the workload's points: the
     first insertion (the half-edge mesh built on the GPU from the resident
@@ -566,8 +650,9 @@ def main():
     ap.add_argument("--workload", default="uniform_2p6m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--legs", default="batched,serving,handle",
-                    help="extra legs in the same line (rank 0, one GPU): batched, serving, handle; '' for none")
+    ap.add_argument("--legs", default="batched,serving,handle,stress",
+                    help="extra legs in the same line (rank 0, one GPU): batched, serving, handle, stress; "
+                         "'' for none")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--no-tune", action="store_true", help="library defaults instead of the autotuner's choice")
     ap.add_argument("--profile-run", choices=["single", "batched"],

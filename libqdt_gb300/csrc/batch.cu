@@ -352,10 +352,13 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_height(Rec* __restrict__ R, int
     NodeOut        o;
     // height 0 is all leaves, the other heights all merges: two kernels, so
     // that neither carries the other's code
+    o.le2 = o.re2 = -1;
+    o.pad0 = o.pad1 = 0;
     if (LEAF || n <= 3)
     {
         if (!LEAF || lane != 0) return;
         B.leaf(lo, hi, V, o.le, o.re);
+        if (d > 0 && !B.bad) extremes_by_walk(B, o.le, o.re, d & 1, 8, o.le2, o.re2);
     }
     else
     {
@@ -382,19 +385,17 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_height(Rec* __restrict__ R, int
             B.fhead = Rn.fhead;
             B.ftail = Rn.ftail;
         }
-        const int lim = 8 * n + 64;
-        int       rl = 0, rr = 0;
+        const int     lim = 8 * n + 64;
+        const int     g = (d - 1) & 1;   // the parent's frame
+        int           rl = 0, rr = 0;
+        ExtremeChoice x{};
+        if (d > 0 && lane == 0) x = extremes_before_merge(B, L, Rn, g);
         if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
         else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
         if (lane != 0) return;
-        if (d > 0 && !B.bad)
-        {
-            const int frame = (d - 1) & 1;
-            const int le2 = B.hull_walk(rl, frame, false, n + 8);
-            const int reccw = B.hull_walk(B.onext(rr), frame, true, n + 8);
-            rl = le2;
-            rr = B.oprev(reccw);
-        }
+        o.le2 = rl;
+        o.re2 = rr;
+        if (d > 0 && !B.bad) extremes_after_merge(B, L, Rn, x, g, n + 8, rl, rr);
         o.le = rl;
         o.re = rr;
     }

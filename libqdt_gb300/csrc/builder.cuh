@@ -286,6 +286,10 @@ struct MapBuilder : Map
     using Map::settle_tail;
     using Map::make_edge;
 
+    // the last merge's lower and upper tangents (its first and last base
+    // edges, both from the right part's vertex to the left part's)
+    int basel_first = -1, basel_last = -1;
+
     __device__ __forceinline__ int     dest(int e) { return org(sym(e)); }
     __device__ __forceinline__ double2 pdest(int e) { return porg(sym(e)); }
     __device__ __forceinline__ int     lnext(int e) { return oprev(sym(e)); }
@@ -446,6 +450,7 @@ struct MapBuilder : Map
     __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
     {
         int basel = tangent(ldo, ldi, rdi, rdo, lim);
+        basel_first = basel_last = basel;
         int it = 0;
         for (;;)
         {
@@ -510,6 +515,7 @@ struct MapBuilder : Map
                 basel = connect(rc, sym(basel));
             else
                 basel = connect(sym(basel), sym(lc));
+            basel_last = basel;
         }
         out_l = ldo;
         out_r = rdo;
@@ -548,6 +554,62 @@ struct MapBuilder : Map
 
 using Builder = MapBuilder<GlobalMap>;
 using CellBuilder = MapBuilder<CellMap>;
+
+// The extremes of a merged node in the frame g of its parent (the reference
+// walks the merged hull to them, builder.hxx:340-346, which takes as many
+// steps as the hull has vertices between the old and the new extremes: all
+// of them for points in convex position). The union's extreme vertex is one
+// of the children's extremes in g, and its hull edge is that child's
+// unless the vertex is a tangent point: with the lower tangent b -> a and
+// the upper tangent d -> c (a, c in the left part), the counter-clockwise
+// hull edge out of a becomes a -> b and out of d becomes d -> c; the
+// clockwise one out of c becomes c -> d and out of b becomes b -> a. Every
+// other hull edge of the children at an extreme vertex lies on the merged
+// hull untouched. The hull walk from that prediction then returns at once
+// with the reference's edge (it walks on if the prediction is off).
+struct ExtremeChoice
+{
+    int  vmin_l, vmin_r, vmax_l, vmax_r;   // the children's extreme vertices in g
+    bool min_right, max_right;             // which child holds the union's
+};
+
+// Read before the merge: it may delete hull edges of the part that does
+// not hold the extreme.
+__device__ inline ExtremeChoice extremes_before_merge(Builder& B, const NodeOut& L, const NodeOut& R, int g)
+{
+    ExtremeChoice x;
+    x.vmin_l = B.org(L.le2);
+    x.vmin_r = B.org(R.le2);
+    x.vmax_l = B.org(L.re2);
+    x.vmax_r = B.org(R.re2);
+    x.min_right = less_frame(B.porg(R.le2), B.porg(L.le2), g);
+    x.max_right = less_frame(B.porg(L.re2), B.porg(R.re2), g);
+    return x;
+}
+
+// After the merge (B.basel_first, B.basel_last set): le and re in frame g,
+// as the reference's hull walks give them.
+__device__ inline void extremes_after_merge(Builder& B, const NodeOut& L, const NodeOut& R, const ExtremeChoice& x,
+    int g, int lim, int& le, int& re)
+{
+    const int b0 = B.basel_first, b1 = B.basel_last;   // b -> a and d -> c
+    int       e;
+    if (!x.min_right) e = x.vmin_l == B.dest(b0) ? sym(b0) : L.le2;
+    else e = x.vmin_r == B.org(b1) ? b1 : R.le2;
+    le = B.hull_walk(e, g, false, lim);
+    if (!x.max_right) e = x.vmax_l == B.dest(b1) ? sym(b1) : L.re2;
+    else e = x.vmax_r == B.org(b0) ? b0 : R.re2;
+    re = B.oprev(B.hull_walk(B.onext(e), g, true, lim));
+}
+
+// A node's extremes in frame g by walking its hull from le, re (a leaf: at
+// most three vertices; a cell root: at most the cell's).
+template <class BuilderT>
+__device__ inline void extremes_by_walk(BuilderT& B, int le, int re, int g, int lim, int& le2, int& re2)
+{
+    le2 = B.hull_walk(le, g, false, lim);
+    re2 = B.oprev(B.hull_walk(B.onext(re), g, true, lim));
+}
 
 // ---------------------------------------------------------------------------
 // Warp-cooperative merge (the upper levels)
@@ -638,6 +700,7 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
     if (lane == 0) basel = B.tangent_one_site(ldo, ldi, rdi, rdo, lim);
     __syncwarp();
     basel = __shfl_sync(FULL, basel, 0);
+    B.basel_first = B.basel_last = basel;
     bool bad = __shfl_sync(FULL, (int)B.bad, 0) != 0;
     // free list: head and the link of the head
     int fhead = __shfl_sync(FULL, B.fhead, 0), ftail = __shfl_sync(FULL, B.ftail, 0);
@@ -821,6 +884,7 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
         B.fhead = fhead;
         B.ftail = ftail;
     }
+    B.basel_last = basel;
     out_l = __shfl_sync(FULL, ldo, 0);
     out_r = __shfl_sync(FULL, rdo, 0);
 }
@@ -983,6 +1047,17 @@ __device__ inline void build_cell(char* smem, const double2* __restrict__ V, Rec
         no.re = ebase + o.re;
         no.fhead = o.fh < 0 ? -1 : rbase + o.fh;
         no.ftail = o.ft < 0 ? -1 : rbase + o.ft;
+        no.le2 = no.re2 = -1;
+        no.pad0 = no.pad1 = 0;
+        if (dc > 0)
+        {
+            // the root's extremes in its own merge frame, walked in shared memory
+            CellBuilder B{ sR, 3 * c, st, pc, -1, -1, false, sV, c };
+            int         le2 = 0, re2 = 0;
+            extremes_by_walk(B, o.le, o.re, dc & 1, c + 8, le2, re2);
+            no.le2 = ebase + le2;
+            no.re2 = ebase + re2;
+        }
         *out = no;
     }
 }

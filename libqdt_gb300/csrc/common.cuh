@@ -33,11 +33,15 @@ struct __align__(16) Rec
 
 // Per-node state handed from a level to its parent level: the two hull edges
 // the reference's build() returns (builder.hxx:303-348), and the node's free
-// list of dead records (head, tail; -1 when empty).
+// list of dead records (head, tail; -1 when empty). le2, re2: the same two
+// edges in the other frame (the one the node itself merged in), from which
+// the parent finds its own extremes without walking its hull.
 struct __align__(16) NodeOut
 {
     int le, re;
     int fhead, ftail;
+    int le2, re2;
+    int pad0, pad1;
 };
 
 // Device status word: bit flags; 0 means fine.
