@@ -385,17 +385,28 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_height(Rec* __restrict__ R, int
             B.fhead = Rn.fhead;
             B.ftail = Rn.ftail;
         }
-        const int     lim = 8 * n + 64;
-        const int     g = (d - 1) & 1;   // the parent's frame
-        int           rl = 0, rr = 0;
-        ExtremeChoice x{};
-        if (d > 0 && lane == 0) x = extremes_before_merge(B, L, Rn, g);
-        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
-        else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
+        const int lim = 8 * n + 64;
+        const int g = (d - 1) & 1;   // the parent's frame
+        int       rl = 0, rr = 0;
+        NodeOut*      self = &out[(1ll << d) + k];
+        volatile int* first = nullptr;
+        if (d > 0 && lane == 0)
+        {
+            extremes_before_merge(R, nrec, st, &out[(2ll << d) + 2 * k], &out[(2ll << d) + 2 * k + 1], self, g);
+            first = lower_tangent_slot(self);
+        }
+        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
+        else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
         if (lane != 0) return;
         o.le2 = rl;
         o.re2 = rr;
-        if (d > 0 && !B.bad) extremes_after_merge(B, L, Rn, x, g, n + 8, rl, rr);
+        if (d > 0 && !B.bad)
+        {
+            const int2 x = extremes_after_merge(R, nrec, st, B.basel_last, self, &out[(2ll << d) + 2 * k],
+                &out[(2ll << d) + 2 * k + 1], g, n + 8);
+            rl = x.x;
+            rr = x.y;
+        }
         o.le = rl;
         o.re = rr;
     }

@@ -286,9 +286,10 @@ struct MapBuilder : Map
     using Map::settle_tail;
     using Map::make_edge;
 
-    // the last merge's lower and upper tangents (its first and last base
-    // edges, both from the right part's vertex to the left part's)
-    int basel_first = -1, basel_last = -1;
+    // the last merge's upper tangent (its last base edge, from the right
+    // part's vertex to the left part's); the lower one goes to memory (the
+    // merge's first_out), so that no register holds it through the merge
+    int basel_last = -1;
 
     __device__ __forceinline__ int     dest(int e) { return org(sym(e)); }
     __device__ __forceinline__ double2 pdest(int e) { return porg(sym(e)); }
@@ -447,10 +448,11 @@ struct MapBuilder : Map
     }
 
     // reference builder.hxx:251-285 (with the scans :205-249 in line)
-    __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
+    __device__ void merge(int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r,
+        volatile int* first_out = nullptr)
     {
         int basel = tangent(ldo, ldi, rdi, rdo, lim);
-        basel_first = basel_last = basel;
+        if (first_out) *first_out = basel;
         int it = 0;
         for (;;)
         {
@@ -515,8 +517,8 @@ struct MapBuilder : Map
                 basel = connect(rc, sym(basel));
             else
                 basel = connect(sym(basel), sym(lc));
-            basel_last = basel;
         }
+        basel_last = basel;
         out_l = ldo;
         out_r = rdo;
     }
@@ -567,39 +569,49 @@ using CellBuilder = MapBuilder<CellMap>;
 // other hull edge of the children at an extreme vertex lies on the merged
 // hull untouched. The hull walk from that prediction then returns at once
 // with the reference's edge (it walks on if the prediction is off).
-struct ExtremeChoice
+//
+// Both steps are out of line and take plain pointers: the merge loop between
+// them keeps its registers. Across the merge the node's own output slot
+// holds the choice (pad0, pad1: the union's extreme vertices in g, bit 31
+// set when the right child holds it) and the lower tangent (le2, written by
+// the merge through its first_out); the slot's final value comes after.
+//
+// Before the merge (it may delete hull edges of the part that does not hold
+// an extreme): the choice, from the children's slots.
+static __device__ __noinline__ void extremes_before_merge(Rec* R, int nrec, DevStatus* st, const NodeOut* Lc,
+    const NodeOut* Rc, NodeOut* self, int g)
 {
-    int  vmin_l, vmin_r, vmax_l, vmax_r;   // the children's extreme vertices in g
-    bool min_right, max_right;             // which child holds the union's
-};
-
-// Read before the merge: it may delete hull edges of the part that does
-// not hold the extreme.
-__device__ inline ExtremeChoice extremes_before_merge(Builder& B, const NodeOut& L, const NodeOut& R, int g)
-{
-    ExtremeChoice x;
-    x.vmin_l = B.org(L.le2);
-    x.vmin_r = B.org(R.le2);
-    x.vmax_l = B.org(L.re2);
-    x.vmax_r = B.org(R.re2);
-    x.min_right = less_frame(B.porg(R.le2), B.porg(L.le2), g);
-    x.max_right = less_frame(B.porg(L.re2), B.porg(R.re2), g);
-    return x;
+    Builder   B{ R, nrec, st, nullptr, -1, -1, false };
+    const int l0 = Lc->le2, l1 = Lc->re2, r0 = Rc->le2, r1 = Rc->re2;
+    const bool min_right = less_frame(B.porg(r0), B.porg(l0), g);
+    const bool max_right = less_frame(B.porg(l1), B.porg(r1), g);
+    const int  vmin = B.org(min_right ? r0 : l0), vmax = B.org(max_right ? r1 : l1);
+    volatile int* p = &self->pad0;
+    p[0] = (int)((unsigned)vmin | (min_right ? 0x80000000u : 0u));
+    p[1] = (int)((unsigned)vmax | (max_right ? 0x80000000u : 0u));
 }
 
-// After the merge (B.basel_first, B.basel_last set): le and re in frame g,
-// as the reference's hull walks give them.
-__device__ inline void extremes_after_merge(Builder& B, const NodeOut& L, const NodeOut& R, const ExtremeChoice& x,
-    int g, int lim, int& le, int& re)
+__device__ __forceinline__ volatile int* lower_tangent_slot(NodeOut* slot) { return &slot->le2; }
+
+// After the merge, with its upper tangent b1: (le, re) in frame g, as the
+// reference's hull walks give them.
+static __device__ __noinline__ int2 extremes_after_merge(Rec* R, int nrec, DevStatus* st, int b1,
+    const NodeOut* self, const NodeOut* Lc, const NodeOut* Rc, int g, int lim)
 {
-    const int b0 = B.basel_first, b1 = B.basel_last;   // b -> a and d -> c
-    int       e;
-    if (!x.min_right) e = x.vmin_l == B.dest(b0) ? sym(b0) : L.le2;
-    else e = x.vmin_r == B.org(b1) ? b1 : R.le2;
-    le = B.hull_walk(e, g, false, lim);
-    if (!x.max_right) e = x.vmax_l == B.dest(b1) ? sym(b1) : L.re2;
-    else e = x.vmax_r == B.org(b0) ? b0 : R.re2;
-    re = B.oprev(B.hull_walk(B.onext(e), g, true, lim));
+    Builder             B{ R, nrec, st, nullptr, -1, -1, false };
+    const volatile int* sp = &self->le2;
+    const int           b0 = sp[0];   // b -> a; b1 is d -> c
+    const int           xmin = sp[2], xmax = sp[3];
+    const bool          min_right = xmin < 0, max_right = xmax < 0;
+    const int           vmin = xmin & 0x7FFFFFFF, vmax = xmax & 0x7FFFFFFF;
+    int                 e;
+    if (!min_right) e = vmin == B.dest(b0) ? sym(b0) : Lc->le2;
+    else e = vmin == B.org(b1) ? b1 : Rc->le2;
+    const int le = B.hull_walk(e, g, false, lim);
+    if (!max_right) e = vmax == B.dest(b1) ? sym(b1) : Lc->re2;
+    else e = vmax == B.org(b0) ? b0 : Rc->re2;
+    const int re = B.oprev(B.hull_walk(B.onext(e), g, true, lim));
+    return make_int2(le, re);
 }
 
 // A node's extremes in frame g by walking its hull from le, re (a leaf: at
@@ -680,7 +692,8 @@ __device__ __forceinline__ double2 shfl_d2(double2 v, int src)
     return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r)
+static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r,
+    volatile int* first_out = nullptr)
 {
     const unsigned FULL = 0xffffffffu;
     Rec* const     R = B.R;
@@ -697,10 +710,13 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
     const int      jj = slot ? j : 0;               // window slot this lane keeps
 
     int basel = 0;
-    if (lane == 0) basel = B.tangent_one_site(ldo, ldi, rdi, rdo, lim);
+    if (lane == 0)
+    {
+        basel = B.tangent_one_site(ldo, ldi, rdi, rdo, lim);
+        if (first_out) *first_out = basel;
+    }
     __syncwarp();
     basel = __shfl_sync(FULL, basel, 0);
-    B.basel_first = B.basel_last = basel;
     bool bad = __shfl_sync(FULL, (int)B.bad, 0) != 0;
     // free list: head and the link of the head
     int fhead = __shfl_sync(FULL, B.fhead, 0), ftail = __shfl_sync(FULL, B.ftail, 0);

@@ -88,18 +88,28 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
             B.fhead = Rn.fhead;
             B.ftail = Rn.ftail;
         }
-        const int     lim = 8 * n + 64;
-        const int     g = (d - 1) & 1;   // the parent's frame
-        int           rl = 0, rr = 0;
-        ExtremeChoice x{};
-        if (d > 0 && lane == 0) x = extremes_before_merge(B, L, Rn, g);
-        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
-        else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr);
+        const int lim = 8 * n + 64;
+        const int g = (d - 1) & 1;   // the parent's frame
+        int       rl = 0, rr = 0;
+        volatile int* first = nullptr;
+        if (d > 0 && lane == 0)
+        {
+            extremes_before_merge(R, nrec, st, &child[2 * k], &child[2 * k + 1], &out[k], g);
+            first = lower_tangent_slot(&out[k]);
+        }
+        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
+        else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
         if (lane != 0) return;
+        // reference builder.hxx:340-346: the extremes in the parent's frame
         o.le2 = rl;
         o.re2 = rr;
-        // reference builder.hxx:340-346: the extremes in the parent's frame
-        if (d > 0 && !B.bad) extremes_after_merge(B, L, Rn, x, g, n + 8, rl, rr);
+        if (d > 0 && !B.bad)
+        {
+            const int2 x =
+                extremes_after_merge(R, nrec, st, B.basel_last, &out[k], &child[2 * k], &child[2 * k + 1], g, n + 8);
+            rl = x.x;
+            rr = x.y;
+        }
         o.le = rl;
         o.re = rr;
     }
