@@ -42,7 +42,7 @@ UNIT = "Mpoints/s"
 # DRAM bytes (read + written) of the build launches of one call, measured with
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum over every k_build_level
 # launch of the second of two `--profile-run single` calls, one pass each)
-BUILD_TRAFFIC = {"uniform_2p6m": 2_600_100_000 + 1_043_000_000}
+BUILD_TRAFFIC = {"uniform_2p6m": 2_716_100_000 + 1_085_800_000}
 
 WORKLOADS = {
     "uniform_2p6m": ("uniform", 2600000, 2),
