@@ -416,6 +416,22 @@ def run_batched_leg(lib, args, flush):
     plain_s = time.perf_counter() - t0
     t.close()
     plain = n / plain_s / 1e6
+    # the CPU port over the same sets: one serial triangulation per set, as
+    # many threads as host cores, each with its own sets (independent
+    # contexts); the oracle releases the GIL inside the C call
+    cpu = None
+    if not args.no_cpu_baseline:
+        from concurrent.futures import ThreadPoolExecutor
+
+        from oracle import oracle as O
+        nt = os.cpu_count() or 1
+        O.lib()   # load once before the threads share it
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=nt) as ex:
+            list(ex.map(lambda s: O.triangulate(s).status, sets, chunksize=16))
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": round(n / cpu_s / 1e6, 3), "s": round(cpu_s, 3), "unit": UNIT, "cores": nt,
+               "kind": "port", "how": "serial port once per set, %d threads with their own sets" % nt}
     return {
         "workload": "4096 sets, log-uniform 16..65536 points, square/disk, 10% on a 256 grid (seed 23)",
         "points": n, "distinct": info["unique_points"], "triangles": info["triangles"],
@@ -425,6 +441,7 @@ def run_batched_leg(lib, args, flush):
         "plain_set_by_set": {"value": round(plain, 3), "s": round(plain_s, 3), "unit": UNIT,
                              "how": "qdt_execute once per set, host buffers"},
         "speedup_e2e_vs_plain": round((n / (e2e / 1e3) / 1e6) / plain, 2),
+        "cpu_port_contexts": cpu,
         "gpu_launches": launches, "exact_violations_sampled": viol, "sampled_sets": len(range(0, len(sets), 64)),
     }
 
@@ -461,7 +478,7 @@ def run_serving_leg(lib, args):
     return out
 
 
-STRESS = ("uniform_1m", "lattice_1024_dups", "gauss_4m", "circle_100k", "line_1m")
+STRESS = ("uniform_100k", "uniform_1m", "lattice_1024_dups", "gauss_4m", "circle_100k", "line_1m")
 
 
 def run_stress_leg(lib, args, flush):
