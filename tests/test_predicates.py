@@ -18,7 +18,7 @@ def _adversarial(kind, n, seed):
     rng = np.random.default_rng(seed)
     k = 3 if kind == "orient" else 4
     out = []
-    per = n // 8
+    per = n // 9
     # 1) uniform in the unit square
     out.append(rng.random((per, k, 2)))
     # 2) nearly collinear / cocircular: lattice points perturbed by a few ulps
@@ -41,6 +41,10 @@ def _adversarial(kind, n, seed):
     t = rng.random((per, k, 1))
     d = rng.standard_normal((per, 1, 2))
     out.append(0.5 + t * d + rng.standard_normal((per, k, 2)) * 2.0 ** -45)
+    # 9) degenerate at float resolution: lattice points moved by a few 2^-30,
+    # below what rounding the coordinates to float keeps
+    base = rng.integers(0, 64, size=(per, k, 2)).astype(np.float64) / 64
+    out.append(base + rng.integers(-4, 5, size=(per, k, 2)) * 2.0 ** -30)
     return np.concatenate(out, axis=0)
 
 
@@ -64,7 +68,7 @@ def test_host_predicates_exact(kind):
     decided = f != 0
     assert np.array_equal(f[decided], want[decided])   # never a wrong sign
     # the uniform block is decided almost always
-    per = pts.shape[0] // 8
+    per = pts.shape[0] // 9
     assert decided[:per].mean() > 0.98
 
 
