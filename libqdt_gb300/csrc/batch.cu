@@ -30,6 +30,7 @@
 #include "context.hpp"
 #include "engine.hpp"
 #include "engine_kernels.hpp"
+#include "host_copy.hpp"
 #include "qdt.h"
 #include "qdt_gpu.h"
 #include "scan.cuh"
@@ -1092,12 +1093,12 @@ qdt_status batch_run(qdtg_batch* b, const qdt_vec2d* pts, bool device_in, const 
             // through page-locked staging in chunks: the host copy of a chunk
             // overlaps the upload of the previous one
             e.h_pts.resize(2 * N);
-            const size_t chunk = (size_t)1 << 18;
+            const size_t chunk = (size_t)1 << 20;   // 16 MiB, each copied by the host pool
             const double* src = reinterpret_cast<const double*>(pts);
             for (size_t o = 0; o < N; o += chunk)
             {
                 const size_t c = std::min(chunk, N - o);
-                std::memcpy(e.h_pts.data() + 2 * o, src + 2 * o, c * sizeof(double2));
+                qdtg::parallel_copy(e.h_pts.data() + 2 * o, src + 2 * o, c * sizeof(double2));
                 cudaMemcpyAsync(e.pts + o, e.h_pts.data() + 2 * o, c * sizeof(double2), cudaMemcpyHostToDevice,
                     e.stream);
             }

@@ -6,6 +6,7 @@
 
 #include "engine.hpp"
 #include "engine_kernels.hpp"
+#include "host_copy.hpp"
 #include "scan.cuh"
 
 namespace qdtg {
@@ -361,11 +362,11 @@ int Engine::run_host(const double* xy, size_t n, PinnedVec<double>& points, Pinn
     rep.resize(n);
     tris.resize(6 * n + 3);
     if (timing_) cudaEventRecord(ev_[0], stream_);
-    const size_t chunk = (size_t)1 << 18;   // points per chunk (4 MiB)
+    const size_t chunk = (size_t)1 << 20;   // points per chunk (16 MiB), each copied by the host pool
     for (size_t off = 0; off < n; off += chunk)
     {
         const size_t c = std::min(chunk, n - off);
-        std::memcpy(points.data() + 2 * off, xy + 2 * off, c * 2 * sizeof(double));
+        parallel_copy(points.data() + 2 * off, xy + 2 * off, c * 2 * sizeof(double));
         cudaMemcpyAsync(w_->pts + off, points.data() + 2 * off, c * sizeof(double2), cudaMemcpyHostToDevice,
             stream_);
     }
