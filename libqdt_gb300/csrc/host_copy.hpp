@@ -13,4 +13,15 @@ namespace qdtg {
 // copies run on the calling thread. Safe to call from several threads.
 void parallel_copy(void* dst, const void* src, size_t bytes) noexcept;
 
+struct CopyItem
+{
+    void*       dst;
+    const void* src;
+    size_t      bytes;
+};
+
+// Copies n independent items (a gather of many small arrays), the items split
+// into groups of about equal bytes over the pool; returns when all are done.
+void parallel_copy_many(const CopyItem* items, size_t n) noexcept;
+
 }  // namespace qdtg

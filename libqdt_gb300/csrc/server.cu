@@ -35,6 +35,7 @@
 
 #include "context.hpp"
 #include "engine.hpp"
+#include "host_copy.hpp"
 #include "qdt.h"
 #include "qdt_gpu.h"
 
@@ -194,6 +195,7 @@ void Server::batch_loop()
     cudaSetDevice(device);
     std::vector<ServeRequest*> take;
     std::vector<size_t>        off;
+    std::vector<CopyItem>      gather;
     for (;;)
     {
         take.clear();
@@ -229,8 +231,10 @@ void Server::batch_loop()
         }
         if (s == QDT_OK)
         {
+            gather.resize(take.size());
             for (size_t i = 0; i < take.size(); ++i)
-                if (take[i]->n) std::memcpy(bpts.data() + 2 * off[i], take[i]->xy, take[i]->n * 2 * sizeof(double));
+                gather[i] = CopyItem{ bpts.data() + 2 * off[i], take[i]->xy, take[i]->n * 2 * sizeof(double) };
+            parallel_copy_many(gather.data(), gather.size());
             s = qdtg_batch_execute(batch, reinterpret_cast<const qdt_vec2d*>(bpts.data()), off.data(), take.size());
         }
         for (size_t i = 0; i < take.size(); ++i)
