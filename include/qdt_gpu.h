@@ -33,6 +33,7 @@ typedef struct qdtg_run_info
     float              ms_h2d, ms_sort, ms_unique, ms_split, ms_build, ms_extract, ms_d2h, ms_total;
     int                device_flags;    /* device status bits; 0 = clean */
     int                kernel_launches; /* kernels the call launched */
+    int                merge_window;    /* candidate window of the warp merges (1 or 2; 0 = none ran) */
 } qdtg_run_info;
 
 /* Options of a context: count_filter_failures != 0 counts the predicate calls
@@ -46,6 +47,13 @@ QDT_API void qdtg_set_options(qdt_t* ptr, int count_filter_failures, int stage_t
    a value out of range or no usable GPU. The triangulation does not depend
    on it. */
 QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points);
+
+/* The candidate window of the context's warp merges: 0 (default) chooses per
+   call from the input -- 1 when most distinct points share their x with
+   another (integer lattices, snapped grids), else 2; 1 or 2 fix it. The
+   triangulation does not depend on it. Returns 1, or 0 for a NULL context,
+   a value out of range or no usable GPU. */
+QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window);
 
 /* Device bytes of a context's workspace for a batch call on n points (the
    workspace is kept between calls and grows when a call needs more). */

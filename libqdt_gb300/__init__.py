@@ -22,7 +22,8 @@ from .qdt_api import (QDT_OK, QDT_ERR_NULL_CONTEXT, QDT_ERR_NULL_ARGUMENT, QDT_E
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
-GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_warp_nodes", "qdtg_set_defaults",
+GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_window", "qdtg_set_warp_nodes",
+               "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
@@ -56,6 +57,7 @@ class RunInfo(ctypes.Structure):
         ("ms_total", ctypes.c_float),
         ("device_flags", ctypes.c_int),
         ("kernel_launches", ctypes.c_int),
+        ("merge_window", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -82,6 +84,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_options.restype = None
     lib.qdtg_set_cell_points.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_cell_points.restype = ctypes.c_int
+    lib.qdtg_set_merge_window.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_merge_window.restype = ctypes.c_int
     lib.qdtg_workspace_bytes.argtypes = [ctypes.c_size_t]
     lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
     lib.qdtg_set_warp_nodes.argtypes = [P, ctypes.c_int]
@@ -197,6 +201,9 @@ class Triangulation(qdt_api.Context):
 
     def set_cell_points(self, cell_points: int) -> bool:
         return self.lib.qdtg_set_cell_points(self.ptr, int(cell_points)) == 1
+
+    def set_merge_window(self, window: int) -> bool:
+        return self.lib.qdtg_set_merge_window(self.ptr, int(window)) == 1
 
     def set_warp_nodes(self, nodes: int) -> bool:
         return self.lib.qdtg_set_warp_nodes(self.ptr, int(nodes)) == 1

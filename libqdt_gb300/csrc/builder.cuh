@@ -652,7 +652,16 @@ __device__ inline void extremes_by_walk(BuilderT& B, int le, int re, int g, int 
 // A scan that deletes its whole window goes on in another pass, without
 // re-testing validity (builder.hxx:216-222). Record indices are clamped to
 // the pool, so no access leaves it; the loops are bounded by guards.
-constexpr int kWin = 2;
+//
+// The window width kWin (1..3, a template parameter: any width gives the
+// same decisions) trades passes against speculative predicate lanes: on
+// points in general position 2 is fastest; on integer lattices and snapped
+// grids, where most speculative in-circle tests are cocircular and go to
+// the exact evaluation side by side in the lanes, 1 is (1024² lattice build
+// 40.5 -> 29.2 ms, 256² grid 11.0 -> 9.4 ms; uniform and circle inputs are
+// 10-25 % slower with 1). The build picks 1 when most distinct points share
+// their x with another (kTieWindow).
+constexpr int kWinDefault = 2;
 
 struct Ent
 {
@@ -692,9 +701,11 @@ __device__ __forceinline__ double2 shfl_d2(double2 v, int src)
     return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
+template <int kWin = kWinDefault>
 static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo, int lim, int& out_l, int& out_r,
     volatile int* first_out = nullptr)
 {
+    static_assert(kWin >= 1 && kWin <= 3, "window of 1 to 3 candidates");
     const unsigned FULL = 0xffffffffu;
     Rec* const     R = B.R;
     const int      nrec = B.nrec;

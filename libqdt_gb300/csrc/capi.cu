@@ -540,6 +540,16 @@ QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
     info->ms_total = r.ms.total;
     info->device_flags = r.device_status;
     info->kernel_launches = r.launches;
+    info->merge_window = r.window;
+    return 1;
+}
+
+QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window)
+{
+    Context* c = ctx(ptr);
+    if (!c || window < 0 || window > 2) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_merge_window(window);
     return 1;
 }
 

@@ -286,6 +286,10 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     b.count_filter = count_filter_ ? 1 : 0;
     b.cell_points = cell_points_;
     b.warp_nodes = warp_nodes_;
+    // lattice-like input (most distinct points share x with another): the
+    // narrow window (builder.cuh, kWinDefault)
+    b.window = window_ ? window_ : (16ull * hs->words[2] > (unsigned long long)kTieWindow * m ? 1 : 2);
+    info_.window = b.window;
     if (m >= 3)
     {
         launch_frames(p, m, s);

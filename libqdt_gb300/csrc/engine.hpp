@@ -80,6 +80,7 @@ struct RunInfo
     StageTimes             ms;
     int                    device_status = 0;
     int                    launches = 0;
+    int                    window = 0;   // warp merges' candidate window of the last call
 };
 
 struct DeviceWork;
@@ -151,6 +152,8 @@ public:
     void            set_cell_points(int c) { cell_points_ = c; }
     int             cell_points() const { return cell_points_; }
     void            set_warp_nodes(int n) { warp_nodes_ = n; }
+    // 0: chosen per call from the input (lattice-like: 1, else 2); 1 or 2: fixed
+    void            set_merge_window(int w) { window_ = w; }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
@@ -166,6 +169,7 @@ private:
     bool            timing_ = false;
     int             cell_points_ = 0;
     int             warp_nodes_ = 4096;
+    int             window_ = 0;
     bool            mesh_source_ = false;   // the device holds the last run_host's points and triangles
     size_t          mesh_n_ = 0, mesh_t_ = 0;
     MeshMirror*     mirror_ = nullptr;

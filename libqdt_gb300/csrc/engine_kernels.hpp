@@ -58,7 +58,13 @@ struct BuildBuffers
     int            count_filter = 0;    // count filter failures in status
     int            cell_points = 0;     // largest cell built in shared memory (0: no cells)
     int            warp_nodes = 4096;   // depths with at most this many nodes: a warp per node
+    int            window = 2;          // the warp merges' candidate window (1 or 2)
 };
+
+// Distinct points sharing x with their predecessor in (x, y) order above
+// this fraction (in 1/16) make the warp merges use a window of one
+// candidate (integer lattices, snapped grids).
+constexpr int kTieWindow = 8;
 
 size_t sort_count_words(size_t n);
 int    split_levels(int m);

@@ -36,8 +36,8 @@ namespace qdtg {
 
 // One depth of the tree: leaves of that depth are built, internal nodes merge
 // their children's results (written by the previous launch). WARP: one node
-// per warp, else one node per thread.
-template <bool WARP>
+// per warp (with a window of WIN candidates), else one node per thread.
+template <bool WARP, int WIN = kWinDefault>
 __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int nrec, const double2* __restrict__ V,
     const NodeOut* __restrict__ child, NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count)
 {
@@ -97,7 +97,7 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
             extremes_before_merge(R, nrec, st, &child[2 * k], &child[2 * k + 1], &out[k], g);
             first = lower_tangent_slot(&out[k]);
         }
-        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
+        if (WARP) warp_merge<WIN>(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
         else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
         if (lane != 0) return;
         // reference builder.hxx:340-346: the extremes in the parent's frame
@@ -246,8 +246,12 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         if ((1ll << d) <= b.warp_nodes)
         {
             const unsigned g = (unsigned)((nodes * 32 + 127) / 128);
-            k_build_level<true><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
-                b.status, b.count_filter);
+            if (b.window == 1)
+                k_build_level<true, 1><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m,
+                    d, b.status, b.count_filter);
+            else
+                k_build_level<true><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
+                    b.status, b.count_filter);
         }
         else
         {

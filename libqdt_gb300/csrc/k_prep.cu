@@ -179,20 +179,27 @@ struct HeadFlag
     }
 };
 
+// Also counts the distinct points that share their x with the previous
+// distinct point (*xties): integer lattices and snapped grids have them in
+// the majority, points in general position almost never, and the build picks
+// its merge window by it.
 __global__ void k_heads(const uint64_t* __restrict__ kx, const uint64_t* __restrict__ ky,
     const uint32_t* __restrict__ idx, const uint32_t* __restrict__ uexcl, const double2* __restrict__ pts, size_t n,
-    uint32_t* __restrict__ head, uint32_t* __restrict__ uid, double2* __restrict__ ucoord)
+    uint32_t* __restrict__ head, uint32_t* __restrict__ uid, double2* __restrict__ ucoord, uint32_t* __restrict__ xties)
 {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (i == 0 || kx[i] != kx[i - 1] || ky[i] != ky[i - 1])
+    bool         tie = false;
+    if (i < n && (i == 0 || kx[i] != kx[i - 1] || ky[i] != ky[i - 1]))
     {
         const uint32_t u = uexcl[i];
         const uint32_t id = idx[i];
         head[u] = (uint32_t)i;
         uid[u] = id;
         ucoord[u] = pts[id];
+        tie = i > 0 && kx[i] == kx[i - 1];
     }
+    const unsigned t = __ballot_sync(0xffffffffu, tie);
+    if ((threadIdx.x & 31) == 0 && t) atomicAdd(xties, (uint32_t)__popc(t));
 }
 
 __global__ void k_rep(const uint64_t* __restrict__ kx, const uint64_t* __restrict__ ky,
@@ -331,7 +338,8 @@ void launch_unique(const PrepBuffers& b, size_t n, cudaStream_t s)
 {
     const int w = b.sorted;
     scan_exclusive(HeadFlag{ b.kx[w], b.ky[w] }, n, b.uexcl, b.scratch, &b.status_u32[0], s);
-    k_heads<<<grid_for(n, 256), 256, 0, s>>>(b.kx[w], b.ky[w], b.val[w], b.uexcl, b.pts, n, b.head, b.uid, b.ucoord);
+    k_heads<<<grid_for(n, 256), 256, 0, s>>>(b.kx[w], b.ky[w], b.val[w], b.uexcl, b.pts, n, b.head, b.uid, b.ucoord,
+        &b.status_u32[2]);
     ++launch_counter();
     k_rep<<<grid_for(n, 256), 256, 0, s>>>(b.kx[w], b.ky[w], b.val[w], b.uexcl, b.uid, n, b.rep);
     ++launch_counter();

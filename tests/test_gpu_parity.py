@@ -141,6 +141,26 @@ def test_cell_sizes_same_result(lib):
             assert not t.set_warp_nodes(0)
 
 
+def test_merge_window_same_result(lib):
+    """The warp merges' candidate window (1 or 2) is a schedule: the same
+    triangulation either way; the automatic choice takes 1 on lattice-like
+    input and 2 on points in general position."""
+    grid = np.round(np.random.default_rng(41).random((40000, 2)) * 96) / 96
+    inputs = [("uniform", W.uniform(80000, 41), 2), ("lattice", W.lattice_with_duplicates(160, 0.02, 42), 1),
+              ("grid", grid, 1), ("circle", W.unit_circle(6000, 43), 2), ("line", W.noisy_line(30000, 44), 2)]
+    for name, p, auto in inputs:
+        want = O.canonical(O.triangulate(p).tris)
+        with G.Triangulation(lib) as t:
+            assert t.set_warp_nodes(1 << 20)   # every depth merges with warps
+            t.set_options(stage_timing=False)
+            for w in (1, 2, 0):
+                assert t.set_merge_window(w)
+                assert t.execute(p) == 0
+                assert np.array_equal(O.canonical(t.triangles_array()), want), (name, w)
+                assert t.run_info()["merge_window"] == (w or auto), (name, w)
+            assert not t.set_merge_window(3)
+
+
 @pytest.mark.parametrize("name", ["gauss_300k", "circle_100k", "line_1m", "lattice_512"])
 def test_exact_checker_zero_violations(lib, name):
     pts = {"gauss_300k": lambda: W.gaussian_mixture(300000, 64, 5),
