@@ -286,7 +286,8 @@ def run_gb300(args):
     # roofline of the dominant stage
     stage_ms = {k: statistics.mean(v) for k, v in stage.items()}
     peak, peak_kind = peaks()
-    # algorithmic bytes per point of each stage ("Roofline")
+    # algorithmic bytes of each stage: the build reads each distinct point
+    # (16 B) and writes the links of its 3 records (32 B each)
     nrec = 3 * m
     alg = {
         "ms_sort": 16 * n + 20 * n + 16 * (16 * n + 40 * n),   # keys + 16 radix passes (hist read, scatter r+w)
