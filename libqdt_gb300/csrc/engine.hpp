@@ -3,6 +3,7 @@
 // host buffers of the context.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <memory>
@@ -90,14 +91,16 @@ size_t bcarve_bytes(size_t N, size_t S);
 
 // Process-wide defaults of the schedule knobs, read when a context, batch or
 // server is created (qdtg_set_defaults; the autotuner sets them).
+// Atomic fields: a thread may set the defaults while another creates a
+// context.
 struct Tuning
 {
-    int cell_points = 0;              // single set: shared-memory cells (0: none)
-    int batch_cell_points = 0;        // many sets: the same
-    int single_warp_nodes = 4096;     // single set: depths of at most this many nodes merge with a warp per node
-    int batch_warp_min_points = 512;  // many sets: heights whose nodes have at least this many points, a warp per node
-    int batch_warp_nodes = 4096;      // many sets: also heights with at most this many nodes
-    int server_large_workers = 4;     // serving: engines for large requests
+    std::atomic<int> cell_points{ 0 };              // single set: shared-memory cells (0: none)
+    std::atomic<int> batch_cell_points{ 0 };        // many sets: the same
+    std::atomic<int> single_warp_nodes{ 4096 };     // single set: depths of at most this many nodes merge with a warp per node
+    std::atomic<int> batch_warp_min_points{ 512 };  // many sets: heights whose nodes have at least this many points, a warp per node
+    std::atomic<int> batch_warp_nodes{ 4096 };      // many sets: also heights with at most this many nodes
+    std::atomic<int> server_large_workers{ 4 };     // serving: engines for large requests
 };
 Tuning& tuning();
 
