@@ -55,6 +55,13 @@ QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points);
    a value out of range or no usable GPU. */
 QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window);
 
+/* The stages after the distinct-point count (split levels, build,
+   extraction: about 250 launches at 2.6 M points) are captured once per
+   (distinct count, knobs) into a CUDA graph and replayed (use_graphs != 0,
+   the default), or launched one by one. The result is the same. Returns 1,
+   or 0 for a NULL context or no usable GPU. */
+QDT_API int qdtg_set_graphs(qdt_t* ptr, int use_graphs);
+
 /* Device bytes of a context's workspace for a batch call on n points (the
    workspace is kept between calls and grows when a call needs more). */
 QDT_API size_t qdtg_workspace_bytes(size_t n);

@@ -22,7 +22,7 @@ from .qdt_api import (QDT_OK, QDT_ERR_NULL_CONTEXT, QDT_ERR_NULL_ARGUMENT, QDT_E
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
-GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_window", "qdtg_set_warp_nodes",
+GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_window", "qdtg_set_graphs", "qdtg_set_warp_nodes",
                "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints",
@@ -86,6 +86,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_cell_points.restype = ctypes.c_int
     lib.qdtg_set_merge_window.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_merge_window.restype = ctypes.c_int
+    lib.qdtg_set_graphs.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_graphs.restype = ctypes.c_int
     lib.qdtg_workspace_bytes.argtypes = [ctypes.c_size_t]
     lib.qdtg_workspace_bytes.restype = ctypes.c_size_t
     lib.qdtg_set_warp_nodes.argtypes = [P, ctypes.c_int]
@@ -204,6 +206,9 @@ class Triangulation(qdt_api.Context):
 
     def set_merge_window(self, window: int) -> bool:
         return self.lib.qdtg_set_merge_window(self.ptr, int(window)) == 1
+
+    def set_graphs(self, on: bool) -> bool:
+        return self.lib.qdtg_set_graphs(self.ptr, int(bool(on))) == 1
 
     def set_warp_nodes(self, nodes: int) -> bool:
         return self.lib.qdtg_set_warp_nodes(self.ptr, int(nodes)) == 1

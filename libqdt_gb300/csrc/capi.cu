@@ -544,6 +544,15 @@ QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
     return 1;
 }
 
+QDT_API int qdtg_set_graphs(qdt_t* ptr, int use_graphs)
+{
+    Context* c = ctx(ptr);
+    if (!c) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_use_graphs(use_graphs != 0);
+    return 1;
+}
+
 QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window)
 {
     Context* c = ctx(ptr);

@@ -155,6 +155,7 @@ Engine::~Engine()
 {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
+    clear_graphs();
     if (w_)
     {
         if (w_->block) cudaFree(w_->block);
@@ -198,6 +199,7 @@ void Engine::release_workspace()
     if (!w_->block) return;
     cudaSetDevice(device_);
     cudaStreamSynchronize(stream_);
+    clear_graphs();
     cudaFree(w_->block);
     w_->block = nullptr;
     w_->cap = 0;
@@ -216,6 +218,7 @@ int Engine::ensure(size_t n)
         w_->block = nullptr;
         w_->cap = 0;
     }
+    clear_graphs();   // they hold pointers into the old workspace
     const size_t bytes = carve(*w_, nullptr, N);
     void*        blk = nullptr;
     if (cudaMalloc(&blk, bytes) != cudaSuccess)
@@ -260,6 +263,28 @@ bool Engine::activate()
 const uint32_t* Engine::device_triangles() const { return w_ ? w_->build.tris : nullptr; }
 const uint32_t* Engine::device_rep() const { return w_ ? w_->prep.rep : nullptr; }
 
+// frames, split levels, leaf order, build, extraction: the stages after the
+// host has read the distinct-point count m (stream order only, no host work)
+void Engine::post_sync_work(size_t m)
+{
+    cudaStream_t  s = stream_;
+    PrepBuffers&  p = w_->prep;
+    BuildBuffers& b = w_->build;
+    launch_frames(p, m, s);
+    launch_split(p, (int)m, s);
+    launch_finalize(p, (int)m, s);
+    if (timing_) cudaEventRecord(ev_[4], s);
+    launch_build(b, (int)m, s);
+    if (timing_) cudaEventRecord(ev_[5], s);
+    launch_extract(b, (int)m, s);
+}
+
+void Engine::clear_graphs() noexcept
+{
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
+    graphs_.clear();
+}
+
 int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep)
 {
     cudaStream_t s = stream_;
@@ -292,13 +317,50 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     info_.window = b.window;
     if (m >= 3)
     {
-        launch_frames(p, m, s);
-        launch_split(p, (int)m, s);
-        launch_finalize(p, (int)m, s);
-        if (timing_) cudaEventRecord(ev_[4], s);
-        launch_build(b, (int)m, s);
-        if (timing_) cudaEventRecord(ev_[5], s);
-        launch_extract(b, (int)m, s);
+        // the stages after the count depend only on m and the knobs: one
+        // CUDA graph per such key (about 250 launches at 2.6 M points)
+        bool ran = false;
+        if (use_graphs_)
+        {
+            const uint64_t key = (uint64_t)m | ((uint64_t)(b.cell_points & 0x7FF) << 32) |
+                                 ((uint64_t)b.window << 43) | ((uint64_t)b.count_filter << 45) |
+                                 ((uint64_t)(timing_ ? 1 : 0) << 46) |
+                                 ((uint64_t)(std::min(b.warp_nodes, (1 << 16) - 1)) << 47);
+            auto it = graphs_.find(key);
+            if (it == graphs_.end())
+            {
+                if (graphs_.size() >= 32) clear_graphs();
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
+                {
+                    const int before = launch_counter();
+                    post_sync_work(m);
+                    const int added = launch_counter() - before;
+                    if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
+                    {
+                        cudaGraphExec_t exec = nullptr;
+                        if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                            it = graphs_.emplace(key, GraphEntry{ exec, added }).first;
+                        cudaGraphDestroy(graph);
+                    }
+                    cudaGetLastError();
+                    launch_counter() = before;   // nothing ran during the capture
+                }
+                else
+                    cudaGetLastError();
+            }
+            if (it != graphs_.end())
+            {
+                if (cudaGraphLaunch(it->second.exec, s) == cudaSuccess)
+                {
+                    ran = true;
+                    launch_counter() += it->second.launches;
+                }
+                else
+                    cudaGetLastError();
+            }
+        }
+        if (!ran) post_sync_work(m);
     }
     else
     {

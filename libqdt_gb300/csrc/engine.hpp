@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <memory>
 #include <new>
+#include <unordered_map>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -157,12 +158,23 @@ public:
     void            set_warp_nodes(int n) { warp_nodes_ = n; }
     // 0: chosen per call from the input (lattice-like: 1, else 2); 1 or 2: fixed
     void            set_merge_window(int w) { window_ = w; }
+    // replay the stages after the distinct-point count from a CUDA graph per
+    // (count, knobs) (default on)
+    void            set_use_graphs(bool on) { use_graphs_ = on; }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
     Engine() = default;
     int  ensure(size_t n);
     int  pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep);
+    void post_sync_work(size_t m);
+    void clear_graphs() noexcept;
+
+    struct GraphEntry
+    {
+        cudaGraphExec_t exec;
+        int             launches;
+    };
 
     int             device_ = 0;
     cudaStream_t    stream_ = nullptr;
@@ -176,6 +188,8 @@ private:
     bool            mesh_source_ = false;   // the device holds the last run_host's points and triangles
     size_t          mesh_n_ = 0, mesh_t_ = 0;
     MeshMirror*     mirror_ = nullptr;
+    bool            use_graphs_ = true;
+    std::unordered_map<uint64_t, GraphEntry> graphs_;   // for the current workspace
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -141,6 +141,28 @@ def test_cell_sizes_same_result(lib):
             assert not t.set_warp_nodes(0)
 
 
+def test_graphs_same_result(lib):
+    """The stages after the distinct-point count replay from a CUDA graph per
+    (count, knobs): sizes that come and go, knob changes between calls and
+    the launch-by-launch form all give the oracle's triangles and the same
+    launch count."""
+    inputs = [W.uniform(70000, 51), W.lattice_with_duplicates(100, 0.02, 52), W.uniform(70000, 53),
+              W.uniform(5000, 54), W.uniform(70000, 51)]
+    with G.Triangulation(lib) as t:
+        for p in inputs:
+            want = O.canonical(O.triangulate(p).tris)
+            got = {}
+            for graphs in (True, False, True):
+                assert t.set_graphs(graphs)
+                for cells, nodes in ((0, 4096), (64, 64)):
+                    assert t.set_cell_points(cells) and t.set_warp_nodes(nodes)
+                    assert t.execute(p) == 0
+                    assert np.array_equal(O.canonical(t.triangles_array()), want), (p.shape, graphs, cells)
+                    got.setdefault((cells, nodes), set()).add(t.run_info()["kernel_launches"])
+            assert all(len(v) == 1 for v in got.values()), got
+        assert t.set_cell_points(0) and t.set_warp_nodes(4096)
+
+
 def test_merge_window_same_result(lib):
     """The warp merges' candidate window (1 or 2) is a schedule: the same
     triangulation either way; the automatic choice takes 1 on lattice-like
