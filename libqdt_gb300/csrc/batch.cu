@@ -560,8 +560,9 @@ struct BatchEngine
     // CUDA graphs of the post-synchronisation part, by batch shape
     struct GraphEntry
     {
-        cudaGraphExec_t exec;
-        int             launches;
+        cudaGraphExec_t       exec;
+        int                   launches;
+        std::vector<uint32_t> shape;   // everything the key hashes, compared on a hit
     };
     static constexpr size_t                  kMaxGraphs = 8;
     std::unordered_map<uint64_t, GraphEntry> graphs;
@@ -921,22 +922,21 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
             cell_block_warps(C) * cell_smem_bytes(C));
 
     // the post-synchronisation launches, replayed from a graph per shape
-    uint64_t key = 1469598103934665603ull;
-    auto     mix = [&](uint64_t v) { key = (key ^ v) * 1099511628211ull; };
-    mix(N);
-    mix(S);
-    mix(count_filter);
-    mix(timing);
-    mix((uint64_t)warp_min_points);
-    mix((uint64_t)warp_nodes);
-    mix((uint64_t)cell_points);
-    for (size_t i = 0; i <= S; ++i) mix(h_u_off[i]);
-    for (size_t i = 0; i < S; ++i) mix(skipv[i]);
     bool ran = false;
     if (use_graph && !timing)
     {
+        std::vector<uint32_t> shape;
+        shape.reserve(2 * S + 8);
+        shape.insert(shape.end(), { (uint32_t)N, (uint32_t)((uint64_t)N >> 32), (uint32_t)S, count_filter ? 1u : 0u,
+                                      (uint32_t)warp_min_points, (uint32_t)warp_nodes, (uint32_t)cell_points });
+        shape.insert(shape.end(), h_u_off.begin(), h_u_off.begin() + S + 1);
+        shape.insert(shape.end(), skipv.begin(), skipv.end());
+        uint64_t key = 1469598103934665603ull;
+        for (uint32_t v : shape) key = (key ^ v) * 1099511628211ull;
         auto it = graphs.find(key);
-        if (it == graphs.end() && graphs.size() < kMaxGraphs)
+        if (it != graphs.end() && it->second.shape != shape)
+            it = graphs.end();   // another shape with the same hash: launch by launch
+        else if (it == graphs.end() && graphs.size() < kMaxGraphs)
         {
             cudaGraph_t graph = nullptr;
             if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
@@ -948,7 +948,7 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
                 {
                     cudaGraphExec_t exec = nullptr;
                     if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
-                        it = graphs.emplace(key, GraphEntry{ exec, added }).first;
+                        it = graphs.emplace(key, GraphEntry{ exec, added, std::move(shape) }).first;
                     cudaGraphDestroy(graph);
                 }
                 cudaGetLastError();

@@ -285,6 +285,48 @@ void Engine::clear_graphs() noexcept
     graphs_.clear();
 }
 
+template <class F>
+void Engine::run_graph(std::pair<uint64_t, uint64_t> key, F&& work)
+{
+    cudaStream_t s = stream_;
+    if (use_graphs_)
+    {
+        auto it = graphs_.find(key);
+        if (it == graphs_.end())
+        {
+            if (graphs_.size() >= 32) clear_graphs();
+            cudaGraph_t graph = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
+            {
+                const int before = launch_counter();
+                work();
+                const int added = launch_counter() - before;
+                if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
+                {
+                    cudaGraphExec_t exec = nullptr;
+                    if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                        it = graphs_.emplace(key, GraphEntry{ exec, added }).first;
+                    cudaGraphDestroy(graph);
+                }
+                cudaGetLastError();
+                launch_counter() = before;   // nothing ran during the capture
+            }
+            else
+                cudaGetLastError();
+        }
+        if (it != graphs_.end())
+        {
+            if (cudaGraphLaunch(it->second.exec, s) == cudaSuccess)
+            {
+                launch_counter() += it->second.launches;   // the kernels recorded in the graph
+                return;
+            }
+            cudaGetLastError();
+        }
+    }
+    work();
+}
+
 int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep)
 {
     cudaStream_t s = stream_;
@@ -294,14 +336,23 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     info_ = RunInfo();
     info_.n = n;
     launch_counter() = 0;
-    if (timing_) cudaEventRecord(ev_[1], s);
-    cudaMemsetAsync(p.status, 0, sizeof(DevStatus), s);
-    cudaMemsetAsync(w_->words, 0, 8 * sizeof(uint32_t), s);
-    launch_keys(p, n, s);
-    launch_sort_points(p, n, s);
-    if (timing_) cudaEventRecord(ev_[2], s);
-    launch_unique(p, n, s);
-    if (timing_) cudaEventRecord(ev_[3], s);
+    // keys, sort, distinct points: one graph per (input size, input array),
+    // as run_device reads the caller's array in place. The array is 16-byte
+    // aligned, so bit 0 set keeps these keys apart from the later stages'
+    // (whose second word has its low four bits clear). The sort's pass count
+    // is fixed, so the buffer it leaves the keys in (p.sorted, set at
+    // capture) is the same on every replay.
+    auto pre_sync = [&] {
+        if (timing_) cudaEventRecord(ev_[1], s);
+        cudaMemsetAsync(p.status, 0, sizeof(DevStatus), s);
+        cudaMemsetAsync(w_->words, 0, 8 * sizeof(uint32_t), s);
+        launch_keys(p, n, s);
+        launch_sort_points(p, n, s);
+        if (timing_) cudaEventRecord(ev_[2], s);
+        launch_unique(p, n, s);
+        if (timing_) cudaEventRecord(ev_[3], s);
+    };
+    run_graph({ ((uint64_t)n << 1) | (timing_ ? 1u : 0u), (uint64_t)(uintptr_t)p.pts | 1u }, pre_sync);
     cudaMemcpyAsync(&hs->st, p.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hs->words, w_->words, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return S_INTERNAL;
@@ -319,48 +370,10 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     {
         // the stages after the count depend only on m and the knobs: one
         // CUDA graph per such key (about 250 launches at 2.6 M points)
-        bool ran = false;
-        if (use_graphs_)
-        {
-            const uint64_t key = (uint64_t)m | ((uint64_t)(b.cell_points & 0x7FF) << 32) |
-                                 ((uint64_t)b.window << 43) | ((uint64_t)b.count_filter << 45) |
-                                 ((uint64_t)(timing_ ? 1 : 0) << 46) |
-                                 ((uint64_t)(std::min(b.warp_nodes, (1 << 16) - 1)) << 47);
-            auto it = graphs_.find(key);
-            if (it == graphs_.end())
-            {
-                if (graphs_.size() >= 32) clear_graphs();
-                cudaGraph_t graph = nullptr;
-                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
-                {
-                    const int before = launch_counter();
-                    post_sync_work(m);
-                    const int added = launch_counter() - before;
-                    if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
-                    {
-                        cudaGraphExec_t exec = nullptr;
-                        if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
-                            it = graphs_.emplace(key, GraphEntry{ exec, added }).first;
-                        cudaGraphDestroy(graph);
-                    }
-                    cudaGetLastError();
-                    launch_counter() = before;   // nothing ran during the capture
-                }
-                else
-                    cudaGetLastError();
-            }
-            if (it != graphs_.end())
-            {
-                if (cudaGraphLaunch(it->second.exec, s) == cudaSuccess)
-                {
-                    ran = true;
-                    launch_counter() += it->second.launches;
-                }
-                else
-                    cudaGetLastError();
-            }
-        }
-        if (!ran) post_sync_work(m);
+        const uint64_t knobs = ((uint64_t)(b.cell_points & 0x7FF) << 4) | ((uint64_t)b.window << 15) |
+                               ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
+                               ((uint64_t)(uint32_t)b.warp_nodes << 20);
+        run_graph({ (uint64_t)m, knobs }, [&] { post_sync_work(m); });
     }
     else
     {

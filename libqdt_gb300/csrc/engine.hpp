@@ -8,7 +8,8 @@
 #include <cstdint>
 #include <memory>
 #include <new>
-#include <unordered_map>
+#include <map>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -169,6 +170,10 @@ private:
     int  pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep);
     void post_sync_work(size_t m);
     void clear_graphs() noexcept;
+    // runs work() on stream(): replayed from the graph cached under key, or
+    // captured into one first; launch by launch when graphs are off or fail
+    template <class F>
+    void run_graph(std::pair<uint64_t, uint64_t> key, F&& work);
 
     struct GraphEntry
     {
@@ -189,7 +194,7 @@ private:
     size_t          mesh_n_ = 0, mesh_t_ = 0;
     MeshMirror*     mirror_ = nullptr;
     bool            use_graphs_ = true;
-    std::unordered_map<uint64_t, GraphEntry> graphs_;   // for the current workspace
+    std::map<std::pair<uint64_t, uint64_t>, GraphEntry> graphs_;   // for the current workspace
     cudaEvent_t     ev_[10] = {};
 };
 

@@ -263,6 +263,23 @@ def test_device_resident_path(lib):
     assert np.array_equal(O.canonical(host), O.canonical(O.triangulate(p).tris))
 
 
+def test_device_arrays_of_one_size(lib):
+    """The device path reads the caller's array in place and the first stages
+    replay from a graph per (size, array): two arrays of one size, each
+    triangulated twice in turn, with host calls of the same size between."""
+    torch = pytest.importorskip("torch")
+    ps = [W.uniform(50000, 91), W.gaussian_mixture(50000, 4, 92)]
+    want = [O.canonical(O.triangulate(p).tris) for p in ps]
+    ds = [torch.from_numpy(p).cuda().contiguous() for p in ps]
+    torch.cuda.synchronize()
+    with G.Triangulation(lib) as t:
+        for i in (0, 1, 0, 1):
+            assert t.execute_device(ds[i].data_ptr(), ps[i].shape[0]) == 0
+            assert np.array_equal(O.canonical(t.download_device_triangles()), want[i]), i
+            assert t.execute(ps[1 - i]) == 0
+            assert np.array_equal(O.canonical(t.triangles_array()), want[1 - i]), i
+
+
 def test_filter_failure_counts(lib):
     with G.Triangulation(lib) as t:
         t.set_options(count_filter_failures=True, stage_timing=True)
