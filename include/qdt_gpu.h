@@ -55,12 +55,24 @@ QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points);
    a value out of range or no usable GPU. */
 QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window);
 
-/* The stages after the distinct-point count (split levels, build,
-   extraction: about 250 launches at 2.6 M points) are captured once per
-   (distinct count, knobs) into a CUDA graph and replayed (use_graphs != 0,
-   the default), or launched one by one. The result is the same. Returns 1,
-   or 0 for a NULL context or no usable GPU. */
+/* The stages before the distinct-point count (keys, sort, distinct points)
+   are captured once per (point count, input array) and the stages after it
+   (split levels, build, extraction: about 250 launches at 2.6 M points)
+   once per (distinct count, knobs) into CUDA graphs and replayed
+   (use_graphs != 0, the default), or launched one by one. The result is
+   the same. Returns 1, or 0 for a NULL context or no usable GPU. */
 QDT_API int qdtg_set_graphs(qdt_t* ptr, int use_graphs);
+
+/* Caps the device bytes of the context's workspace (0: no cap, the
+   default). A batch call whose workspace would exceed the cap returns
+   QDT_ERR_OUT_OF_MEMORY and leaves the context empty, as when cudaMalloc
+   fails; a workspace already above a new cap is freed. The device copy of
+   the mesh (qdtg_locate_points) is not counted. Returns 1, or 0 for a NULL
+   context or no usable GPU. */
+QDT_API int qdtg_set_workspace_limit(qdt_t* ptr, size_t bytes);
+
+/* Device bytes the context's workspace holds now (0 when none). */
+QDT_API size_t qdtg_context_workspace_bytes(const qdt_t* ptr);
 
 /* Device bytes of a context's workspace for a batch call on n points (the
    workspace is kept between calls and grows when a call needs more). */

@@ -72,7 +72,12 @@ def load_cached(lib) -> dict | None:
 
 def _best_build_ms(run, calls: int = 3) -> float:
     run()   # warm-up (workspace allocation, first-touch)
-    return min(run() for _ in range(calls))
+    best = min(run() for _ in range(calls))
+    if not best > 0:
+        # a zero build time means the stage events did not record: choosing
+        # by it would pick an arbitrary candidate
+        raise RuntimeError("autotune: the build stage timed at %r ms" % best)
+    return best
 
 
 def tune(lib, verbose: bool = False) -> dict:

@@ -553,6 +553,21 @@ QDT_API int qdtg_set_graphs(qdt_t* ptr, int use_graphs)
     return 1;
 }
 
+QDT_API int qdtg_set_workspace_limit(qdt_t* ptr, size_t bytes)
+{
+    Context* c = ctx(ptr);
+    if (!c) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_workspace_limit(bytes);
+    return 1;
+}
+
+QDT_API size_t qdtg_context_workspace_bytes(const qdt_t* ptr)
+{
+    const Context* c = ctx(ptr);
+    return (c && c->engine) ? c->engine->workspace_bytes() : 0;
+}
+
 QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window)
 {
     Context* c = ctx(ptr);

@@ -189,6 +189,7 @@ size_t Engine::bytes_after(size_t n) const
     if (w_->block && n <= w_->cap) return w_->bytes;
     size_t N = std::max<size_t>(n, 1024);
     if (w_->cap) N = std::max(N, w_->cap + w_->cap / 4);
+    if (limit_ && workspace_bytes(N) > limit_) N = std::max<size_t>(n, 1024);
     return workspace_bytes(N);
 }
 
@@ -206,11 +207,23 @@ void Engine::release_workspace()
     w_->bytes = 0;
 }
 
+void Engine::set_workspace_limit(size_t bytes)
+{
+    limit_ = bytes;
+    if (limit_ && w_->block && w_->bytes > limit_) release_workspace();
+}
+
 int Engine::ensure(size_t n)
 {
     if (n <= w_->cap && w_->block) return S_OK;
     size_t N = std::max<size_t>(n, 1024);
     if (w_->cap) N = std::max(N, w_->cap + w_->cap / 4);
+    if (limit_ && workspace_bytes(N) > limit_)
+    {
+        // grow to the exact size instead, or fail with the old workspace kept
+        N = std::max<size_t>(n, 1024);
+        if (workspace_bytes(N) > limit_) return S_OOM;
+    }
     if (w_->block)
     {
         cudaStreamSynchronize(stream_);
@@ -273,9 +286,9 @@ void Engine::post_sync_work(size_t m)
     launch_frames(p, m, s);
     launch_split(p, (int)m, s);
     launch_finalize(p, (int)m, s);
-    if (timing_) cudaEventRecord(ev_[4], s);
+    mark(4);
     launch_build(b, (int)m, s);
-    if (timing_) cudaEventRecord(ev_[5], s);
+    mark(5);
     launch_extract(b, (int)m, s);
 }
 
@@ -283,6 +296,18 @@ void Engine::clear_graphs() noexcept
 {
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
     graphs_.clear();
+}
+
+// A stage-timing event. Recorded on a capturing stream, a plain
+// cudaEventRecord only orders the capture and is not replayed: the external
+// flag makes it an event-record node of the graph.
+void Engine::mark(int i)
+{
+    if (!timing_) return;
+    if (capturing_)
+        cudaEventRecordWithFlags(ev_[i], stream_, cudaEventRecordExternal);
+    else
+        cudaEventRecord(ev_[i], stream_);
 }
 
 template <class F>
@@ -299,7 +324,9 @@ void Engine::run_graph(std::pair<uint64_t, uint64_t> key, F&& work)
             if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
             {
                 const int before = launch_counter();
+                capturing_ = true;
                 work();
+                capturing_ = false;
                 const int added = launch_counter() - before;
                 if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
                 {
@@ -343,14 +370,14 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     // is fixed, so the buffer it leaves the keys in (p.sorted, set at
     // capture) is the same on every replay.
     auto pre_sync = [&] {
-        if (timing_) cudaEventRecord(ev_[1], s);
+        mark(1);
         cudaMemsetAsync(p.status, 0, sizeof(DevStatus), s);
         cudaMemsetAsync(w_->words, 0, 8 * sizeof(uint32_t), s);
         launch_keys(p, n, s);
         launch_sort_points(p, n, s);
-        if (timing_) cudaEventRecord(ev_[2], s);
+        mark(2);
         launch_unique(p, n, s);
-        if (timing_) cudaEventRecord(ev_[3], s);
+        mark(3);
     };
     run_graph({ ((uint64_t)n << 1) | (timing_ ? 1u : 0u), (uint64_t)(uintptr_t)p.pts | 1u }, pre_sync);
     cudaMemcpyAsync(&hs->st, p.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);

@@ -133,6 +133,9 @@ public:
     size_t        workspace_bytes() const;
     // frees the workspace (the next call allocates it again)
     void          release_workspace();
+    // caps the workspace's device bytes (0: none); a call that needs more
+    // returns QDT_ERR_OUT_OF_MEMORY; a workspace above a new cap is freed
+    void          set_workspace_limit(size_t bytes);
 
     // The half-edge mesh of the last run_host result (n points, T triangles),
     // built on the device (k_mesh.cu). Returns 0, or a negative value when
@@ -174,6 +177,7 @@ private:
     // captured into one first; launch by launch when graphs are off or fail
     template <class F>
     void run_graph(std::pair<uint64_t, uint64_t> key, F&& work);
+    void mark(int i);   // records stage-timing event i when timing is on
 
     struct GraphEntry
     {
@@ -194,6 +198,8 @@ private:
     size_t          mesh_n_ = 0, mesh_t_ = 0;
     MeshMirror*     mirror_ = nullptr;
     bool            use_graphs_ = true;
+    size_t          limit_ = 0;   // workspace bytes cap (0: none)
+    bool            capturing_ = false;   // run_graph is recording stream_
     std::map<std::pair<uint64_t, uint64_t>, GraphEntry> graphs_;   // for the current workspace
     cudaEvent_t     ev_[10] = {};
 };

@@ -209,6 +209,34 @@ def test_not_finite_and_recovery(lib):
         assert np.array_equal(O.canonical(t.triangles_array()), O.canonical(O.triangulate(p).tris))
 
 
+def test_workspace_limit_out_of_memory(lib):
+    """Allocation failure driven from the host: a workspace cap below what a
+    call needs gives QDT_ERR_OUT_OF_MEMORY and an empty context, calls that
+    fit still run, and lifting the cap recovers."""
+    big, small = W.uniform(100000, 61), W.uniform(1000, 62)
+    need = lib.qdtg_workspace_bytes(100000)
+    want_big = O.canonical(O.triangulate(big).tris)
+    want_small = O.canonical(O.triangulate(small).tris)
+    with G.Triangulation(lib) as t:
+        assert t.set_workspace_limit(need - 1)
+        assert t.execute(big) == Q.QDT_ERR_OUT_OF_MEMORY
+        assert t.points_size() == 0 and t.triangles_size() == 0
+        assert t.execute(small) == 0
+        assert np.array_equal(O.canonical(t.triangles_array()), want_small)
+        assert 0 < t.workspace_bytes() < need
+        assert t.execute(big, parallel=True) == Q.QDT_ERR_OUT_OF_MEMORY
+        assert t.set_workspace_limit(need)          # exactly enough: no growth margin
+        assert t.execute(big) == 0 and t.workspace_bytes() == need
+        assert np.array_equal(O.canonical(t.triangles_array()), want_big)
+        assert t.set_workspace_limit(lib.qdtg_workspace_bytes(2000))   # frees the larger workspace
+        assert t.workspace_bytes() == 0
+        assert t.execute(small) == 0
+        assert np.array_equal(O.canonical(t.triangles_array()), want_small)
+        assert t.set_workspace_limit(0)
+        assert t.execute(big) == 0
+        assert np.array_equal(O.canonical(t.triangles_array()), want_big)
+
+
 def test_input_is_copied(lib):
     p = np.array([[0.0, 0.0], [4.0, 0.0], [3.0, 1.0], [1.0, 1.0]])
     keep = p.copy()
@@ -290,3 +318,11 @@ def test_filter_failure_counts(lib):
         assert t.execute(W.uniform(100000, 4)) == 0
         info = t.run_info()
         assert info["incircle_exact"] == 0
+        # stage times come from events inside the replayed graphs too
+        for graphs in (True, False):
+            assert t.set_graphs(graphs)
+            for _ in range(2):
+                assert t.execute(W.uniform(100000, 4)) == 0
+                info = t.run_info()
+                for k in ("ms_sort", "ms_unique", "ms_split", "ms_build", "ms_extract"):
+                    assert info[k] > 0, (graphs, k, info[k])
