@@ -37,6 +37,18 @@ namespace qdtg {
 using MV = MeshVertex;
 using HE = MeshHalfEdge;
 
+// Start points of the host walks: a uniform grid over the vertices' bounding
+// box, about two vertices per cell, holding one vertex of each cell.
+// Vertices are never removed, so a seed never goes stale. Built once the
+// walks without it have taken about as many steps as building it costs.
+struct SeedGrid
+{
+    int              gx = 0, gy = 0;
+    double           x0 = 0, y0 = 0, ix = 0, iy = 0;
+    std::vector<int> cell;         // vertex per cell, -1 when none
+    size_t           walked = 0;   // walk steps taken before the grid existed
+};
+
 struct Mesh
 {
     MeshVec<MV>      v;
@@ -44,6 +56,7 @@ struct Mesh
     std::vector<int> free_h;
     MeshVec<int>     o2l;    // point index -> mesh vertex, -1 when none
     std::vector<int> t2h;    // triangle -> one of its half-edges
+    SeedGrid         grid;
     int              last = 0;
     uint64_t         id = next_id();   // identifies this mesh to the device mirror
     uint64_t         version = 0;      // bumped by every call that may change the mesh
@@ -235,7 +248,7 @@ void remove_tri(Context& c, Mesh& M, size_t idx)
 // Returns a half-edge of the triangle containing p (border included), or -1
 // with *hull set to a hull half-edge that p sees. The walk starts at the
 // half-edge `start` when it is alive, else at the last insertion.
-int locate(const Mesh& M, size_t ntri, double px, double py, int* hull, int start = -1)
+int locate(const Mesh& M, size_t ntri, double px, double py, int* hull, int start = -1, size_t* steps = nullptr)
 {
     *hull = -1;
     if (M.h.empty() || ntri == 0) return -1;
@@ -248,6 +261,7 @@ int locate(const Mesh& M, size_t ntri, double px, double py, int* hull, int star
     }
     for (size_t step = 0; step < ntri + 16; ++step)
     {
+        if (steps) *steps = step + 1;
         const int h0 = h, h1 = M.h[h0].next, h2 = M.h[h1].next;
         if (M.h[h2].next != h0) break;
         const int o0 = orient(M, M.h[h0].org, M.h[h1].org, px, py);
@@ -281,6 +295,105 @@ int locate(const Mesh& M, size_t ntri, double px, double py, int* hull, int star
         }
     }
     return -1;
+}
+
+size_t seed_cell(const SeedGrid& g, double x, double y)
+{
+    const double fx = (x - g.x0) * g.ix, fy = (y - g.y0) * g.iy;
+    const int    cx = fx >= g.gx - 1 ? g.gx - 1 : (fx > 0 ? (int)fx : 0);
+    const int    cy = fy >= g.gy - 1 ? g.gy - 1 : (fy > 0 ? (int)fy : 0);
+    return (size_t)cy * (size_t)g.gx + (size_t)cx;
+}
+
+void seed_build(Mesh& M)
+{
+    SeedGrid& g = M.grid;
+    if (M.v.empty()) return;
+    double x0 = M.v[0].x, x1 = x0, y0 = M.v[0].y, y1 = y0;
+    for (const MV& p : M.v)
+    {
+        x0 = std::min(x0, p.x), x1 = std::max(x1, p.x);
+        y0 = std::min(y0, p.y), y1 = std::max(y1, p.y);
+    }
+    const double w = x1 - x0, hgt = y1 - y0;
+    const double cells = std::max(1.0, std::min((double)M.v.size() / 2.0, (double)(1 << 24)));
+    int          gx = 1, gy = 1;
+    if (w > 0 && hgt > 0 && std::isfinite(w) && std::isfinite(hgt))
+    {
+        gx = (int)std::clamp(std::sqrt(cells * w / hgt), 1.0, cells);
+        gy = (int)std::clamp(cells / gx, 1.0, cells);
+    }
+    else if (w > 0 && std::isfinite(w))
+        gx = (int)cells;
+    else if (hgt > 0 && std::isfinite(hgt))
+        gy = (int)cells;
+    g.gx = gx;
+    g.gy = gy;
+    g.x0 = x0;
+    g.y0 = y0;
+    g.ix = (gx > 1 && w > 0 && std::isfinite(gx / w)) ? gx / w : 0.0;
+    g.iy = (gy > 1 && hgt > 0 && std::isfinite(gy / hgt)) ? gy / hgt : 0.0;
+    g.cell.assign((size_t)gx * (size_t)gy, -1);
+    for (size_t i = 0; i < M.v.size(); ++i) g.cell[seed_cell(g, M.v[i].x, M.v[i].y)] = (int)i;
+    // an empty cell (about one in seven at two vertices per cell) takes the
+    // nearest seed along its row, or of the nearest row that has one
+    std::vector<char> row_has(gy, 0);
+    for (int y = 0; y < gy; ++y)
+    {
+        int* row = g.cell.data() + (size_t)y * gx;
+        int  last = -1;
+        for (int x = 0; x < gx; ++x)
+        {
+            if (row[x] >= 0)
+                last = row[x];
+            else
+                row[x] = last;
+        }
+        last = -1;
+        for (int x = gx - 1; x >= 0; --x)
+        {
+            if (row[x] >= 0)
+                last = row[x];
+            else
+                row[x] = last;
+        }
+        row_has[y] = row[0] >= 0;
+    }
+    for (int pass = 0; pass < 2; ++pass)
+    {
+        int src = -1;
+        for (int k = 0; k < gy; ++k)
+        {
+            const int y = pass ? gy - 1 - k : k;
+            if (row_has[y])
+                src = y;
+            else if (src >= 0)
+            {
+                std::copy_n(g.cell.data() + (size_t)src * gx, gx, g.cell.data() + (size_t)y * gx);
+                row_has[y] = 1;
+            }
+        }
+    }
+}
+
+// A half-edge out of the seed vertex of p's cell, or -1 (no grid yet, empty
+// cell); any live half-edge is a valid start for locate()
+int seed_start(const Mesh& M, double x, double y)
+{
+    if (M.grid.cell.empty()) return -1;
+    const int v = M.grid.cell[seed_cell(M.grid, x, y)];
+    if (v < 0 || v >= (int)M.v.size()) return -1;
+    const int he = M.v[v].he;
+    return (he >= 0 && he < (int)M.h.size() && M.h[he].org == v) ? he : -1;
+}
+
+// counts a walk's steps while there is no grid; builds the grid once the
+// walks have cost about as much as the build (one pass over the vertices)
+void seed_account(Mesh& M, size_t steps)
+{
+    if (!M.grid.cell.empty()) return;
+    M.grid.walked += steps;
+    if (M.grid.walked > M.v.size() / 32 + 64) seed_build(M);
 }
 
 // Flips the diagonal h (Wrapper.cpp:942-1009). Before: triangles
@@ -463,8 +576,11 @@ int mesh_insert_point(Context& c, double x, double y, bool, int hint)
     if (M.h.empty()) return insert_by_rebuild(c, x, y);
     ++M.version;
 
-    int hull = -1;
-    int h_start = locate(M, c.ntris(), x, y, &hull, hint);
+    int    hull = -1;
+    size_t steps = 0;
+    if (hint < 0) hint = seed_start(M, x, y);
+    int h_start = locate(M, c.ntris(), x, y, &hull, hint, &steps);
+    seed_account(M, steps);
     if (h_start < 0 && hull < 0) return insert_by_rebuild(c, x, y);
     const bool outside = h_start < 0;
     if (!outside)
@@ -502,6 +618,7 @@ int mesh_insert_point(Context& c, double x, double y, bool, int hint)
     M.v.push_back(MV{ x, y, id, -1 });
     if (M.o2l.size() <= id) M.o2l.resize(id + 1, -1);
     M.o2l[id] = nv;
+    if (!M.grid.cell.empty()) M.grid.cell[seed_cell(M.grid, x, y)] = nv;
 
     // visible hull edges (outside case)
     std::vector<int> visible;

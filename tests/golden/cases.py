@@ -163,4 +163,21 @@ def mesh_cases():
             else:
                 ops.append(("constraint", int(rng.integers(0, n + 5)), int(rng.integers(0, n + 5))))
         out.append(("mixed_%d" % s, p, ops))
+    # long runs of single insertions: enough walk steps that the host's seed
+    # grid of walk starts is built part-way through (uniform points with
+    # insertions partly outside the hull; an integer lattice with insertions
+    # on its vertices, on its edges and outside)
+    rng = np.random.default_rng(7100)
+    p = rng.random((4000, 2))
+    ops = [("insert", float(x), float(y)) for x, y in rng.random((300, 2)) * 1.2 - 0.1]
+    out.append(("long_uniform", p, ops))
+    g = np.stack(np.meshgrid(np.arange(40.0), np.arange(40.0)), axis=-1).reshape(-1, 2)
+    ops = []
+    for k in range(300):
+        i, j = (float(v) for v in rng.integers(0, 40, size=2))
+        kind = k % 4
+        q = (i, j) if kind == 0 else ((i + 0.5, j) if kind == 1 else ((i + 0.25, j + 0.75) if kind == 2 else
+                                                                      (i * 1.5 - 10.0, j - 45.0)))
+        ops.append(("insert", q[0], q[1]))
+    out.append(("long_lattice", g, ops))
     return out

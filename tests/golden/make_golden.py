@@ -41,9 +41,8 @@ from tests.golden import cases as C  # noqa: E402
 _dump = None
 
 
-def run_ref(lib, pts, parallel):
-    """Runs the reference's batch call and reads the context back through its
-    query functions (in bulk, via oracle/qdt_dump.c)."""
+def load_dump():
+    """The bulk readers of a reference context (oracle/qdt_dump.c)."""
     global _dump
     import ctypes
     if _dump is None:
@@ -52,6 +51,13 @@ def run_ref(lib, pts, parallel):
         _dump.qdt_dump_triangles.restype = ctypes.c_size_t
         _dump.qdt_dump_used.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _dump.qdt_dump_used.restype = ctypes.c_size_t
+    return _dump
+
+
+def run_ref(lib, pts, parallel):
+    """Runs the reference's batch call and reads the context back through its
+    query functions (in bulk, via oracle/qdt_dump.c)."""
+    load_dump()
     with Q.Context(lib) as c:
         st = c.execute(pts, parallel=parallel)
         tris = np.zeros((c.triangles_size(), 3), dtype=np.int64)
@@ -70,9 +76,10 @@ def main():
         print("reference not available; nothing generated")
         return 1
     lib = Q.load(O.REF_LIB_PATH)
+    mesh_only = "--mesh-only" in sys.argv   # regenerate mesh_cases.npz alone
 
     small = {}
-    for name, pts in C.small_cases():
+    for name, pts in ([] if mesh_only else C.small_cases()):
         st, tris, used = run_ref(lib, pts, False)
         st2, tris2, used2 = run_ref(lib, pts, True)
         ct = O.canonical(tris)
@@ -82,10 +89,12 @@ def main():
         small[name + "/pts"] = pts
         small[name + "/tris"] = ct.astype(np.int64)
         small[name + "/used"] = used
-    np.savez_compressed(os.path.join(HERE, "small_cases.npz"), **small)
-    print("small cases:", len(small) // 3)
+    if not mesh_only:
+        np.savez_compressed(os.path.join(HERE, "small_cases.npz"), **small)
+        print("small cases:", len(small) // 3)
 
     mesh = {}
+    load_dump()
     for name, pts, ops in C.mesh_cases():
         for par in (False, True):
             with Q.Context(lib) as c:
@@ -111,6 +120,8 @@ def main():
             mesh[key + "/used"] = used
     np.savez_compressed(os.path.join(HERE, "mesh_cases.npz"), **mesh)
     print("mesh cases:", len(mesh) // 3)
+    if mesh_only:
+        return 0
 
     out = {"canonical_form": "qdt_verify.cpp:408-427", "cases": []}
     for spec in C.large_specs():

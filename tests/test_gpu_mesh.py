@@ -76,7 +76,7 @@ def constrained_valid(t, cons):
 def test_mesh_cases_equal_reference(lib):
     d = np.load(os.path.join(GOLDEN, "mesh_cases.npz"))
     for name, pts, ops in C.mesh_cases():
-        general = name.startswith(("six_point", "quad")) or (name.startswith("mixed_") and
+        general = name.startswith(("six_point", "quad", "long_uniform")) or (name.startswith("mixed_") and
                                                             int(name.split("_")[1]) % 3 == 0)
         for par in (False, True):
             key = "%s/%s" % (name, "par" if par else "ser")
