@@ -63,6 +63,12 @@ QDT_API int qdtg_set_merge_window(qdt_t* ptr, int window);
    the same. Returns 1, or 0 for a NULL context or no usable GPU. */
 QDT_API int qdtg_set_graphs(qdt_t* ptr, int use_graphs);
 
+/* The Dwyer split levels below the first depth whose nodes hold at most
+   4,096 points run in one launch, a thread block per node working in shared
+   memory (on != 0, the default), or one level at a time. The result is the
+   same. Returns 1, or 0 for a NULL context or no usable GPU. */
+QDT_API int qdtg_set_split_tail(qdt_t* ptr, int on);
+
 /* Caps the device bytes of the context's workspace (0: no cap, the
    default). A batch call whose workspace would exceed the cap returns
    QDT_ERR_OUT_OF_MEMORY and leaves the context empty, as when cudaMalloc

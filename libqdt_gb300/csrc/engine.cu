@@ -389,6 +389,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     b.count_filter = count_filter_ ? 1 : 0;
     b.cell_points = cell_points_;
     b.warp_nodes = warp_nodes_;
+    p.split_tail = split_tail_;
     // lattice-like input (most distinct points share x with another): the
     // narrow window (builder.cuh, kWinDefault)
     b.window = window_ ? window_ : (16ull * hs->words[2] > (unsigned long long)kTieWindow * m ? 1 : 2);
@@ -399,6 +400,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         // CUDA graph per such key (about 250 launches at 2.6 M points)
         const uint64_t knobs = ((uint64_t)(b.cell_points & 0x7FF) << 4) | ((uint64_t)b.window << 15) |
                                ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
+                               ((uint64_t)(p.split_tail ? 1 : 0) << 19) |
                                ((uint64_t)(uint32_t)b.warp_nodes << 20);
         run_graph({ (uint64_t)m, knobs }, [&] { post_sync_work(m); });
     }

@@ -165,6 +165,9 @@ public:
     // replay the stages after the distinct-point count from a CUDA graph per
     // (count, knobs) (default on)
     void            set_use_graphs(bool on) { use_graphs_ = on; }
+    // run the split depths of nodes of at most 4,096 points in one
+    // shared-memory launch (default on)
+    void            set_split_tail(bool on) { split_tail_ = on; }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
@@ -198,6 +201,7 @@ private:
     size_t          mesh_n_ = 0, mesh_t_ = 0;
     MeshMirror*     mirror_ = nullptr;
     bool            use_graphs_ = true;
+    bool            split_tail_ = true;
     size_t          limit_ = 0;   // workspace bytes cap (0: none)
     bool            capturing_ = false;   // run_graph is recording stream_
     std::map<std::pair<uint64_t, uint64_t>, GraphEntry> graphs_;   // for the current workspace

@@ -32,6 +32,7 @@ struct PrepBuffers
     uint32_t*      A[2] = { nullptr, nullptr };
     uint32_t*      B[2] = { nullptr, nullptr };
     int            acur = 0, bcur = 0;
+    bool           split_tail = true;   // the depths of small nodes in one shared-memory launch
     uint8_t*       side = nullptr;      // m
     double*        seam = nullptr;      // 2^(kSeamDepth+1): cut coordinate per upper node
     unsigned long long* box = nullptr;  // 4: bounding box of the points as order keys (min x, min y, max x, max y)

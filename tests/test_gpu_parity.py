@@ -163,6 +163,28 @@ def test_graphs_same_result(lib):
         assert t.set_cell_points(0) and t.set_warp_nodes(4096)
 
 
+def test_split_tail_same_result(lib):
+    """The split depths of nodes of at most 4,096 points run in one
+    shared-memory launch or one level at a time: the same triangles (the
+    oracle's), sizes on both sides of the block limit, degenerate inputs."""
+    rng = np.random.default_rng(81)
+    inputs = [W.uniform(n, 80 + n) for n in (4, 5, 7, 8, 100, 4095, 4096, 4097, 8192, 8193, 12289, 70000)]
+    inputs += [W.lattice_with_duplicates(90, 0.05, 82), W.unit_circle(9000, 83), W.noisy_line(20000, 84),
+               np.round(rng.random((30000, 2)) * 64) / 64]
+    with G.Triangulation(lib) as t:
+        for p in inputs:
+            want = O.canonical(O.triangulate(p).tris)
+            launches = {}
+            for tail in (True, False, True):
+                assert t.set_split_tail(tail)
+                assert t.execute(p) == 0
+                assert np.array_equal(O.canonical(t.triangles_array()), want), (p.shape, tail)
+                launches.setdefault(tail, set()).add(t.run_info()["kernel_launches"])
+            assert len(launches[True]) == 1
+            if p.shape[0] > 4:
+                assert min(launches[True]) < min(launches[False]), (p.shape, launches)
+
+
 def test_merge_window_same_result(lib):
     """The warp merges' candidate window (1 or 2) is a schedule: the same
     triangulation either way; the automatic choice takes 1 on lattice-like
