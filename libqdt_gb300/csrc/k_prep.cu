@@ -165,6 +165,84 @@ static void radix_sort(uint64_t* khi[2], uint64_t* klo[2], uint32_t* val[2], siz
 
 size_t sort_count_words(size_t n) { return (size_t)256 * ((n + kSortTile - 1) / kSortTile) + 1; }
 
+// Small inputs: one block sorts in shared memory (bitonic network over the
+// next power of two, padded with keys above every real one) and writes the
+// result where the radix passes would leave it (an even pass count ends in
+// buffer 0). Keys are made unique by the value, so the order is the stable
+// radix sort's: (khi, klo, val) ascending for the points; for the frame-1
+// order, (klo ascending, val descending), the stable sort of the reversed
+// (x, y) order that k_frame1_keys sets up.
+constexpr int kSmallSort = 4096;
+constexpr int kSmallThreads = 1024;
+
+template <int KW>
+__global__ void __launch_bounds__(kSmallThreads) k_small_sort(uint64_t* khi, uint64_t* klo, uint32_t* val, int n)
+{
+    extern __shared__ uint64_t ssort[];
+    int P = 1;
+    while (P < n) P <<= 1;
+    uint64_t* hi = ssort;
+    uint64_t* lo = hi + (KW == 2 ? kSmallSort : 0);
+    uint32_t* v = reinterpret_cast<uint32_t*>(lo + kSmallSort);
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+    {
+        const bool real = i < n;
+        if (KW == 2) hi[i] = real ? khi[i] : ~0ull;
+        lo[i] = real ? klo[i] : ~0ull;
+        // padding sorts last: above every real value in both orders
+        v[i] = real ? val[i] : (KW == 2 ? 0xFFFFFFFFu : 0u);
+    }
+    __syncthreads();
+    auto before = [&](int x, int y) -> bool {   // element x precedes element y
+        if (KW == 2)
+        {
+            if (hi[x] != hi[y]) return hi[x] < hi[y];
+            if (lo[x] != lo[y]) return lo[x] < lo[y];
+            return v[x] < v[y];
+        }
+        if (lo[x] != lo[y]) return lo[x] < lo[y];
+        return v[x] > v[y];
+    };
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1)
+        {
+            for (int t = threadIdx.x; t < P / 2; t += blockDim.x)
+            {
+                const int  x = 2 * t - (t & (j - 1));   // lower index of the pair (x, x + j)
+                const int  y = x + j;
+                const bool up = (x & k) == 0;
+                if (before(y, x) == up)
+                {
+                    if (KW == 2)
+                    {
+                        const uint64_t h = hi[x];
+                        hi[x] = hi[y];
+                        hi[y] = h;
+                    }
+                    const uint64_t l = lo[x];
+                    lo[x] = lo[y];
+                    lo[y] = l;
+                    const uint32_t w = v[x];
+                    v[x] = v[y];
+                    v[y] = w;
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+    {
+        if (KW == 2) khi[i] = hi[i];
+        klo[i] = lo[i];
+        val[i] = v[i];
+    }
+}
+
+template <int KW>
+constexpr int small_sort_smem()
+{
+    return kSmallSort * (KW * 8 + 4);
+}
+
 // ---------------------------------------------------------------------------
 // K1: unique points, representatives
 // ---------------------------------------------------------------------------
@@ -481,7 +559,14 @@ void launch_keys(const PrepBuffers& b, size_t n, cudaStream_t s)
 void launch_sort_points(PrepBuffers& b, size_t n, cudaStream_t s)
 {
     int which = 0;
-    radix_sort<2>(b.kx, b.ky, b.val, n, &which, b.counts, b.offs, b.scratch, s);
+    if (n > 1 && n <= (size_t)kSmallSort)
+    {
+        cudaFuncSetAttribute(k_small_sort<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, small_sort_smem<2>());
+        k_small_sort<2><<<1, kSmallThreads, small_sort_smem<2>(), s>>>(b.kx[0], b.ky[0], b.val[0], (int)n);
+        ++launch_counter();
+    }
+    else
+        radix_sort<2>(b.kx, b.ky, b.val, n, &which, b.counts, b.offs, b.scratch, s);
     b.sorted = which;
 }
 
@@ -509,7 +594,14 @@ void launch_frames(PrepBuffers& b, size_t m, cudaStream_t s)
     k_frame1_keys<<<grid_for(m, 256), 256, 0, s>>>(b.ky[w], b.head, m, k1[0], v1[0]);
     ++launch_counter();
     int which = 0;
-    radix_sort<1>(nullptr, k1, v1, m, &which, b.counts, b.offs, b.scratch, s);
+    if (m > 1 && m <= (size_t)kSmallSort)
+    {
+        cudaFuncSetAttribute(k_small_sort<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, small_sort_smem<1>());
+        k_small_sort<1><<<1, kSmallThreads, small_sort_smem<1>(), s>>>(nullptr, k1[0], v1[0], (int)m);
+        ++launch_counter();
+    }
+    else
+        radix_sort<1>(nullptr, k1, v1, m, &which, b.counts, b.offs, b.scratch, s);
     b.bcur = which;
     b.acur = 0;
 }
