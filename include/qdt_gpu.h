@@ -138,8 +138,9 @@ QDT_API qdt_status qdtg_trace_constraints(qdt_t* ptr, const qdt_edge* edges, siz
     int64_t* crossed);
 
 /* The context's build merges with a whole warp per node at the depths that
-   have at most warp_nodes nodes (few merges: each one's latency counts) and
-   with one thread per node below (many merges); default 4096. Returns 1, or
+   have at most warp_nodes nodes (few merges: each one's latency counts) or
+   whose nodes hold at least 192 points, and with one thread per node below
+   (many small merges); default 4096. Returns 1, or
    0 for a NULL context, a value below 1 or no usable GPU. The triangulation
    does not depend on it. */
 QDT_API int qdtg_set_warp_nodes(qdt_t* ptr, int warp_nodes);

@@ -67,6 +67,10 @@ struct BuildBuffers
 // candidate (integer lattices, snapped grids).
 constexpr int kTieWindow = 8;
 
+// Single-set build: depths whose nodes hold at least this many points merge
+// with a warp per node whatever the warp-node threshold (m >> d points).
+constexpr int kWarpMinPoints = 192;
+
 size_t sort_count_words(size_t n);
 int    split_levels(int m);
 

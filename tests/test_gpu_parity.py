@@ -134,7 +134,7 @@ def test_cell_sizes_same_result(lib):
                 assert np.array_equal(O.canonical(t.triangles_array()), want), (p.shape, c)
             assert not t.set_cell_points(3) and not t.set_cell_points(1025)
             assert t.set_cell_points(0)
-            for nodes in (1, 64, 1 << 20):       # warp merges from none to every depth
+            for nodes in (1, 64, 1 << 20):       # warp merges from the fewest depths to every depth
                 assert t.set_warp_nodes(nodes)
                 assert t.execute(p) == 0
                 assert np.array_equal(O.canonical(t.triangles_array()), want), (p.shape, nodes)
