@@ -34,6 +34,7 @@
 #include "qdt.h"
 #include "qdt_gpu.h"
 #include "scan.cuh"
+#include "split_tail.cuh"
 
 namespace qdtg {
 
@@ -251,6 +252,7 @@ struct BNode
 {
     int lo, hi;   // global positions
     int dep;
+    int tail;     // the set's tail depth: the depths from there run in k_bsplit_tail
 };
 __device__ __forceinline__ BNode bnode_of(const uint32_t* __restrict__ useg, const uint32_t* __restrict__ u_off,
     int i, int d)
@@ -262,6 +264,7 @@ __device__ __forceinline__ BNode bnode_of(const uint32_t* __restrict__ useg, con
     b.dep = node_of(ms, d, i - base, lo, hi);
     b.lo = lo + base;
     b.hi = hi + base;
+    b.tail = tail_depth(ms);
     return b;
 }
 
@@ -272,8 +275,33 @@ __global__ void k_bsplit_mark(const uint32_t* __restrict__ S, uint8_t* __restric
     if (i >= (int)M) return;
     const BNode b = bnode_of(useg, u_off, i, d);
     uint8_t     s = 0;
-    if (b.dep == d && b.hi - b.lo >= 4) s = (i >= b.lo + (b.hi - b.lo) / 2) ? 1 : 0;
+    if (b.dep == d && d < b.tail && b.hi - b.lo >= 4) s = (i >= b.lo + (b.hi - b.lo) / 2) ? 1 : 0;
     side[S[i]] = s;
+}
+
+// the split depths of a set from its tail depth down (or, for a set the
+// build skips, a copy of its slice), one block per entry (split_tail.cuh)
+constexpr uint32_t kTailCopy = 0xFFFFFFFFu;
+__global__ void __launch_bounds__(kTailThreads) k_bsplit_tail(const uint32_t* Ain, const uint32_t* Bin,
+    uint32_t* Aout, uint32_t* Bout, uint32_t* __restrict__ loc, const uint2* __restrict__ ent,
+    const uint32_t* __restrict__ u_off, uint32_t M)
+{
+    extern __shared__ uint32_t tsm[];
+    const uint2 e = ent[blockIdx.x];
+    const int   base = (int)u_off[e.x], ms = (int)(u_off[e.x + 1] - u_off[e.x]);
+    if (e.y == kTailCopy)
+    {
+        for (int j = threadIdx.x; j < ms; j += blockDim.x)
+        {
+            if (Ain != Aout) Aout[base + j] = Ain[base + j];
+            if (Bin != Bout) Bout[base + j] = Bin[base + j];
+        }
+        return;
+    }
+    const int t = tail_depth(ms);
+    int       lo, hi;
+    node_at(ms, t, e.y, lo, hi);
+    split_tail_node(Ain, Bin, Aout, Bout, loc, nullptr, nullptr, ms, base, lo, hi, t, split_depth(ms), M, tsm);
 }
 
 struct BSideOf
@@ -291,7 +319,7 @@ __global__ void k_bsplit_scatter(const uint32_t* __restrict__ O, uint32_t* __res
     if (j >= (int)M) return;
     const BNode    b = bnode_of(useg, u_off, j, d);
     const uint32_t p = O[j];
-    if (b.dep != d || b.hi - b.lo < 4)
+    if (b.dep != d || d >= b.tail || b.hi - b.lo < 4)
     {
         O2[j] = p;
         return;
@@ -538,6 +566,12 @@ struct BatchEngine
     uint32_t *counts = nullptr, *offs = nullptr, *scratch = nullptr, *words = nullptr;
     DevStatus* status = nullptr;
     size_t     nodes_cap = 0;
+    // split tails: one entry (set, node of the set's tail depth, or
+    // kTailCopy) per block; the per-depth launches run the depths above
+    uint2*             tail = nullptr;
+    size_t             tail_cap = 0;
+    std::vector<uint2> h_tail;
+    int                tail_levels = 0;   // depths of the per-depth launches
     // host results (pinned)
     PinnedVec<uint32_t> h_tris, h_rep, h_tri_base, h_u_off, h_in_off;
     PinnedVec<double>   h_pts;   // staging of host input
@@ -653,6 +687,10 @@ size_t bcarve(BatchEngine& g, char* base, size_t N, size_t S)
     // node heaps: sum over sets of 2^(D+1) <= 4 N + 2 S
     g.nodes_cap = 4 * N + 2 * S + 16;
     g.nodes = c.take<NodeOut>(g.nodes_cap);
+    // split tails: a set of m points has 2^tail_depth(m) < 2 m / kTailMax
+    // tail nodes when it has more than one
+    g.tail_cap = S + 2 * N / kTailMax + 16;
+    g.tail = c.take<uint2>(g.tail_cap);
     return c.off + 256;
 }
 
@@ -727,9 +765,10 @@ void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax)
             cudaMemcpyAsync(Bv[0], v1[cur], M * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
         }
     }
-    // split levels
-    int acur = 0, bcur = 0;
-    for (int d = 0; d < Dmax; ++d)
+    // split levels: per depth down to the deepest tail depth, then the tails
+    int       acur = 0, bcur = 0;
+    const int Dper = std::min(tail_levels, Dmax);
+    for (int d = 0; d < Dper; ++d)
     {
         const int axis = d & 1;
         uint32_t* Sa = axis == 0 ? A[acur] : Bv[bcur];
@@ -742,6 +781,22 @@ void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax)
         k_bsplit_scatter<<<gridn(M, 256), 256, 0, s>>>(O, O2, side, uexcl, useg, u_off, M, d);
         ++launch_counter();
         ocur = 1 - ocur;
+    }
+    if (!h_tail.empty())
+    {
+        const uint32_t* Ain = A[acur];
+        const uint32_t* Bin = Bv[bcur];
+        // end in the buffers the depth-by-depth form ends in
+        for (int d = Dper; d < Dmax; ++d)
+        {
+            int& ocur = (d & 1) == 0 ? bcur : acur;
+            ocur = 1 - ocur;
+        }
+        cudaFuncSetAttribute(k_bsplit_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem);
+        // the split ranks in uexcl are spent: it holds the local ids
+        k_bsplit_tail<<<(unsigned)h_tail.size(), kTailThreads, kTailSmem, s>>>(Ain, Bin, A[acur], Bv[bcur], uexcl,
+            tail, u_off, M);
+        ++launch_counter();
     }
     k_bfinalize<<<gridn(M, 256), 256, 0, s>>>(A[acur], Bv[bcur], ucoord, uid, useg, u_off, M, V, vid);
     ++launch_counter();
@@ -879,6 +934,22 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
     h_cell_off[S] = (uint32_t)cacc;
     ncells = (uint32_t)cacc;
     if (nacc > nodes_cap || cacc > 0xFFFFFFFFull) return QDT_ERR_INTERNAL;
+    // split tails: every set's slice is written by its entries (a copy for
+    // the sets the build skips)
+    h_tail.clear();
+    tail_levels = 0;
+    for (size_t i = 0; i < S; ++i)
+    {
+        if (skipv[i])
+        {
+            h_tail.push_back(make_uint2((uint32_t)i, kTailCopy));
+            continue;
+        }
+        const int t = tail_depth((int)(h_u_off[i + 1] - h_u_off[i]));
+        tail_levels = std::max(tail_levels, t);
+        for (uint32_t k = 0; k < (1u << t); ++k) h_tail.push_back(make_uint2((uint32_t)i, k));
+    }
+    if (h_tail.size() > tail_cap || h_tail.size() > 0x7FFFFFFFull) return QDT_ERR_INTERNAL;
     // per height the entries (set, depth) that hold nodes of that height (at
     // depths D - h and D - h - 1, above the cells), with their slot offsets
     int Hmax = -1;
@@ -913,6 +984,7 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
     if (h_ents.size() > kEntWords * (capS + 1) || h_eoffs.size() > kEntWords * (capS + 1) || S >= (1u << 27))
         return QDT_ERR_INTERNAL;
     cudaMemcpyAsync(skip, skipv.data(), S, cudaMemcpyHostToDevice, s);
+    if (!h_tail.empty()) cudaMemcpyAsync(tail, h_tail.data(), h_tail.size() * sizeof(uint2), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(noff, h_noff.data(), (S + 1) * 4, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(cell_off, h_cell_off.data(), (S + 1) * 4, cudaMemcpyHostToDevice, s);
     if (!h_ents.empty()) cudaMemcpyAsync(ents, h_ents.data(), h_ents.size() * 4, cudaMemcpyHostToDevice, s);

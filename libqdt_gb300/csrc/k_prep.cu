@@ -16,6 +16,7 @@
 #include "common.cuh"
 #include "engine_kernels.hpp"
 #include "scan.cuh"
+#include "split_tail.cuh"
 
 namespace qdtg {
 
@@ -377,154 +378,16 @@ __global__ void k_split_scatter(const uint32_t* __restrict__ O, uint32_t* __rest
 }
 
 // The levels below the first depth d0 whose nodes hold at most kTailMax
-// points, in shared memory: one block per node of depth d0 runs the depths
-// d0..D-1 with the marks of k_split_mark (seam coordinates included) and the
-// stable partitions of k_split_scatter, on its slice of both orders, and
-// writes the final orders once. Inside the block the points go by local ids
-// (their frame-0 positions in the slice), so the side flags and both orders
-// live in shared memory; loc (m words of scratch) maps a point to its local
-// id once. Ain/Aout (and Bin/Bout) may be the same buffer: a block reads its
-// whole slice before it writes it.
-constexpr int kTailThreads = 512;
-constexpr int kTailItems = 8;
-constexpr int kTailMax = kTailThreads * kTailItems;
-constexpr int kTailSmem = kTailMax * (4 + 3 * 2 + 2 + 1) + 64 * 4;
-
-// the node of depth at most d0 + levels holding position i, from the node
-// [lo, hi) down (the halving of node_of); returns the levels descended
-__device__ __forceinline__ int node_below(int lo, int hi, int levels, int i, int& nlo, int& nhi)
-{
-    for (int l = 0; l < levels; ++l)
-    {
-        if (hi - lo < 4)
-        {
-            nlo = lo, nhi = hi;
-            return l;
-        }
-        const int mid = lo + (hi - lo) / 2;
-        if (i < mid) hi = mid;
-        else lo = mid;
-    }
-    nlo = lo, nhi = hi;
-    return levels;
-}
-
+// points: one block per node of depth d0 (split_tail.cuh), seam
+// coordinates included.
 __global__ void __launch_bounds__(kTailThreads) k_split_tail(const uint32_t* Ain, const uint32_t* Bin, uint32_t* Aout,
     uint32_t* Bout, uint32_t* __restrict__ loc, const double2* __restrict__ ucoord, double* __restrict__ seam, int m,
     int d0, int D)
 {
     extern __shared__ uint32_t tsm[];
-    uint32_t* gid = tsm;                                            // point of each local id
-    uint32_t* ssm = tsm + kTailMax;                                 // block scan
-    uint16_t* a = reinterpret_cast<uint16_t*>(ssm + 64);            // frame-0 order (local ids)
-    uint16_t* b = a + kTailMax;                                     // frame-1 order
-    uint16_t* t = b + kTailMax;                                     // partition target
-    uint16_t* r = t + kTailMax;                                     // right-side points before each position
-    uint8_t*  side = reinterpret_cast<uint8_t*>(r + kTailMax);      // by local id
-    int       lo = 0, hi = m;
-    for (int l = 0; l < d0; ++l)
-    {
-        const int mid = lo + (hi - lo) / 2;
-        if ((blockIdx.x >> (d0 - 1 - l)) & 1u) lo = mid;
-        else hi = mid;
-    }
-    const int sz = hi - lo;
-    if (sz > kTailMax) return;   // the host sizes d0 so that this never holds
-    for (int j = threadIdx.x; j < sz; j += blockDim.x)
-    {
-        const uint32_t p = Ain[lo + j];
-        gid[j] = p;
-        a[j] = (uint16_t)j;
-        if (p < (uint32_t)m) loc[p] = (uint32_t)j;
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < sz; j += blockDim.x)
-    {
-        const uint32_t p = Bin[lo + j];
-        const uint32_t l = p < (uint32_t)m ? loc[p] : 0u;
-        b[j] = (uint16_t)(l < (uint32_t)sz ? l : 0u);   // always in range: both orders hold the node's points
-    }
-    __syncthreads();
-    const int base = threadIdx.x * kTailItems;
-    for (int d = d0; d < D; ++d)
-    {
-        uint16_t* S = (d & 1) ? b : a;
-        uint16_t* O = (d & 1) ? a : b;
-        for (int j = threadIdx.x; j < sz; j += blockDim.x)
-        {
-            const int i = lo + j;
-            int       nlo, nhi;
-            const int dep = d0 + node_below(lo, hi, d - d0, i, nlo, nhi);
-            uint8_t   s = 0;
-            if (dep == d && nhi - nlo >= 4)
-            {
-                const int mid = nlo + (nhi - nlo) / 2;
-                s = (i >= mid) ? 1 : 0;
-                if (i == mid && d <= kSeamDepth)
-                {
-                    long long k = 0;
-                    int       x = 0, y = m;
-                    for (int l = 0; l < d; ++l)
-                    {
-                        const int c = x + (y - x) / 2;
-                        if (i < c) y = c, k = 2 * k;
-                        else x = c, k = 2 * k + 1;
-                    }
-                    const double2 p = ucoord[min(gid[S[j]], (uint32_t)m - 1)];
-                    seam[(1ll << d) + k] = (d & 1) ? p.y : p.x;
-                }
-            }
-            side[S[j]] = s;
-        }
-        __syncthreads();
-        uint32_t cnt = 0;
-        for (int q = 0; q < kTailItems; ++q)
-            if (base + q < sz) cnt += side[O[base + q]];
-        uint32_t total;
-        uint32_t run = block_excl_scan(cnt, ssm, &total);
-        for (int q = 0; q < kTailItems; ++q)
-            if (base + q < sz)
-            {
-                r[base + q] = (uint16_t)run;
-                run += side[O[base + q]];
-            }
-        __syncthreads();
-        for (int q = 0; q < kTailItems; ++q)
-        {
-            const int j = base + q;
-            if (j >= sz) break;
-            int            nlo, nhi;
-            const int      dep = d0 + node_below(lo, hi, d - d0, lo + j, nlo, nhi);
-            const uint16_t p = O[j];
-            if (dep != d || nhi - nlo < 4)
-            {
-                t[j] = p;
-                continue;
-            }
-            const int l0 = nlo - lo, mid = l0 + (nhi - nlo) / 2;
-            const int rb = (int)(uint16_t)(r[j] - r[l0]);
-            const int to = side[p] ? mid + rb : l0 + (j - l0 - rb);
-            if (to >= 0 && to < sz) t[to] = p;   // always: both orders hold the node's points
-        }
-        __syncthreads();
-        if (d & 1)
-        {
-            uint16_t* x = a;
-            a = t;
-            t = x;
-        }
-        else
-        {
-            uint16_t* x = b;
-            b = t;
-            t = x;
-        }
-    }
-    for (int j = threadIdx.x; j < sz; j += blockDim.x)
-    {
-        Aout[lo + j] = gid[a[j]];
-        Bout[lo + j] = gid[b[j]];
-    }
+    int lo, hi;
+    node_at(m, d0, blockIdx.x, lo, hi);
+    split_tail_node(Ain, Bin, Aout, Bout, loc, ucoord, seam, m, 0, lo, hi, d0, D, (uint32_t)m, tsm);
 }
 
 // V in leaf order: inside a leaf the points follow the frame of its parent's
@@ -624,7 +487,7 @@ void launch_split(PrepBuffers& b, int m, cudaStream_t s)
     // the first depth whose nodes all fit one shared-memory block (D: none)
     int d0 = 0;
     if (b.split_tail)
-        while (d0 < D && (((long long)m + (1ll << d0) - 1) >> d0) > kTailMax) ++d0;
+        d0 = std::min(D, tail_depth(m));
     else
         d0 = D;
     for (int d = 0; d < d0; ++d)
