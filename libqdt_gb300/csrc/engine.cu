@@ -135,6 +135,18 @@ Engine* Engine::create(int* cuda_error)
     }
     for (auto& ev : g->ev_)
         cudaEventCreate(&ev);
+    // the build's prefetch stream; without it the prefetch runs in line
+    if (cudaStreamCreateWithFlags(&g->side_, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->fork_, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->join_, cudaEventDisableTiming) != cudaSuccess)
+    {
+        cudaGetLastError();
+        if (g->side_) cudaStreamDestroy(g->side_);
+        if (g->fork_) cudaEventDestroy(g->fork_);
+        if (g->join_) cudaEventDestroy(g->join_);
+        g->side_ = nullptr;
+        g->fork_ = g->join_ = nullptr;
+    }
     g->w_ = new (std::nothrow) DeviceWork();
     g->mirror_ = new (std::nothrow) MeshMirror();
     if (!g->w_ || !g->mirror_)
@@ -155,6 +167,7 @@ Engine::~Engine()
 {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
+    if (side_) cudaStreamSynchronize(side_);
     clear_graphs();
     if (w_)
     {
@@ -169,6 +182,9 @@ Engine::~Engine()
     }
     for (auto& ev : ev_)
         if (ev) cudaEventDestroy(ev);
+    if (fork_) cudaEventDestroy(fork_);
+    if (join_) cudaEventDestroy(join_);
+    if (side_) cudaStreamDestroy(side_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -389,6 +405,9 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     b.count_filter = count_filter_ ? 1 : 0;
     b.cell_points = cell_points_;
     b.warp_nodes = warp_nodes_;
+    b.side = side_;
+    b.fork = fork_;
+    b.join = join_;
     p.split_tail = split_tail_;
     // lattice-like input (most distinct points share x with another): the
     // narrow window (builder.cuh, kWinDefault)

@@ -190,6 +190,8 @@ private:
 
     int             device_ = 0;
     cudaStream_t    stream_ = nullptr;
+    cudaStream_t    side_ = nullptr;   // the build's seam prefetch beside the merges
+    cudaEvent_t     fork_ = nullptr, join_ = nullptr;
     DeviceWork*     w_ = nullptr;
     RunInfo         info_;
     bool            count_filter_ = false;

@@ -60,6 +60,10 @@ struct BuildBuffers
     int            cell_points = 0;     // largest cell built in shared memory (0: no cells)
     int            warp_nodes = 4096;   // depths with at most this many nodes: a warp per node
     int            window = 2;          // the warp merges' candidate window (1 or 2)
+    // a second stream for the seam prefetch of the next depth beside the
+    // merges of this one (none: the prefetch runs in line)
+    cudaStream_t   side = nullptr;
+    cudaEvent_t    fork = nullptr, join = nullptr;
 };
 
 // Distinct points sharing x with their predecessor in (x, y) order above

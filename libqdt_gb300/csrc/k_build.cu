@@ -227,21 +227,39 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         k_seam_band<<<1, 1, 0, s>>>(b.box, m, const_cast<double*>(b.seam));
         ++launch_counter();
     }
+    // the seam prefetch of depth pd on stream ps: the list lives in the
+    // extraction's offsets (3 m words, unused until the extraction) and its
+    // length in the triangle counter (written by the extraction's scan)
+    auto prefetch_depth = [&](int pd, cudaStream_t ps) {
+        uint32_t* const list = b.tri_off;
+        uint32_t* const count = b.tri_count;
+        cudaMemsetAsync(count, 0, sizeof(uint32_t), ps);
+        k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, ps>>>(b.recs, nrec, m, pd, b.seam, list, count,
+            (uint32_t)nrec);
+        k_prefetch_list<<<152 * 8, 256, 0, ps>>>(b.recs, list, count, (uint32_t)nrec);
+        launch_counter() += 2;
+    };
+    // With a side stream, the prefetch of depth d - 1 runs beside the merges
+    // of depth d (a few SMs), and depth d - 1 waits for it; it reads records
+    // those merges may be editing, which only makes a hint less exact.
+    const bool overlap = prefetch && b.side && b.fork && b.join;
+    bool       pending = false;
     for (int d = D; d >= 0; --d)
     {
         const long long nodes = 1ll << d;
         if (d <= kSeamDepth && prefetch)
         {
-            // the list lives in the extraction's offsets (3 m words, unused
-            // until the extraction) and its length in the triangle counter
-            // (written by the extraction's scan)
-            uint32_t* const list = b.tri_off;
-            uint32_t* const count = b.tri_count;
-            cudaMemsetAsync(count, 0, sizeof(uint32_t), s);
-            k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, s>>>(b.recs, nrec, m, d, b.seam, list, count,
-                (uint32_t)nrec);
-            k_prefetch_list<<<152 * 8, 256, 0, s>>>(b.recs, list, count, (uint32_t)nrec);
-            launch_counter() += 2;
+            if (pending) cudaStreamWaitEvent(s, b.join, 0);
+            else prefetch_depth(d, s);
+            pending = false;
+        }
+        if (overlap && d >= 1 && d - 1 <= kSeamDepth)
+        {
+            cudaEventRecord(b.fork, s);
+            cudaStreamWaitEvent(b.side, b.fork, 0);
+            prefetch_depth(d - 1, b.side);
+            cudaEventRecord(b.join, b.side);
+            pending = true;
         }
         // a warp per merge at the depths with at most warp_nodes nodes, and
         // at those whose nodes hold at least kWarpMinPoints points (the 4 M
