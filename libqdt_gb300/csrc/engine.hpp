@@ -168,6 +168,9 @@ public:
     // run the split depths of nodes of at most 4,096 points in one
     // shared-memory launch (default on)
     void            set_split_tail(bool on) { split_tail_ = on; }
+    // the build's seam prefetch on a second stream beside the merges, when
+    // no other engine is running a call (default on)
+    void            set_side_prefetch(bool on) { side_prefetch_ = on; }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
@@ -204,6 +207,7 @@ private:
     MeshMirror*     mirror_ = nullptr;
     bool            use_graphs_ = true;
     bool            split_tail_ = true;
+    bool            side_prefetch_ = true;
     size_t          limit_ = 0;   // workspace bytes cap (0: none)
     bool            capturing_ = false;   // run_graph is recording stream_
     std::map<std::pair<uint64_t, uint64_t>, GraphEntry> graphs_;   // for the current workspace

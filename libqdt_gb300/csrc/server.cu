@@ -123,6 +123,8 @@ void Server::large_loop(ServeWorker* w)
     cv_done.notify_all();
     if (!w->eng) return;
     w->eng->set_cell_points(cfg.cell_points);
+    // the server's engines share the GPU: the build's prefetch in line
+    w->eng->set_side_prefetch(false);
     for (;;)
     {
         ServeRequest* r = nullptr;
