@@ -218,22 +218,24 @@ QDT_API int qdtg_eval_predicates(int kind, int mode, int on_device, const double
 
 /* Distinct points and representatives of n device-resident points, with no
    device allocation at all. This entry point has no counterpart in the
-   reference. It is meant for callers that cannot call cudaMalloc: code that
-   records a CUDA graph that must not allocate, plug-ins whose host
-   application owns every device allocation, real-time loops that may not
-   take the allocator's locks or latency. It computes the batch path's first
-   stage (the reference's load_unique_points): d_rep[i] receives the lowest
-   index j with the same coordinates as point i (-0.0 equals +0.0), and
-   *unique_points the number of distinct points.
+   reference. It is meant for callers that cannot call cudaMalloc: plug-ins
+   whose host application owns every device allocation, real-time loops that
+   may not take the allocator's locks or latency. It computes the batch
+   path's first stage (the reference's load_unique_points): d_rep[i]
+   receives the lowest index j with the same coordinates as point i (-0.0
+   equals +0.0), and *unique_points the number of distinct points.
    Limit: n <= 65536; larger n returns QDT_ERR_TOO_MANY_POINTS and does
    nothing. QDT_ERR_NULL_ARGUMENT for NULL pointers, QDT_ERR_NOT_FINITE for a
    NaN or infinite coordinate (d_rep is then not written), QDT_ERR_INTERNAL
-   for a CUDA failure. The work runs on cuda_stream (a cudaStream_t, NULL for
-   the default stream) and the call returns when it is done.
+   for a CUDA failure or a stream of another device than the current one.
+   The work runs on cuda_stream (a cudaStream_t of the current device, NULL
+   for the default stream); the call copies its status into host memory and
+   waits for the stream before it returns.
    Its working memory (2.6 MB) is a static array of the library on each GPU,
    kept until the process exits and shared by every call: calls that overlap
-   on the GPU race, so serialise them. The first call on a device looks up the
-   array's device address; make that first call before any stream capture. */
+   on the GPU race, so serialise them. The first call on a device looks up
+   the array's device address; make that first call before any stream
+   capture begins. */
 QDT_API qdt_status qdtg_unique_points_noalloc(const qdt_vec2d* d_pts, size_t n, uint32_t* d_rep,
     size_t* unique_points, void* cuda_stream);
 

@@ -1,8 +1,7 @@
 // Distinct points and representatives without any device allocation.
 //
-// Some callers cannot call cudaMalloc at all: code that runs while a stream
-// is being captured into a CUDA graph that must not allocate, plug-ins whose
-// host application owns every device allocation and forbids others, and
+// Some callers cannot call cudaMalloc at all: plug-ins whose host
+// application owns every device allocation and forbids others, and
 // real-time loops that may not take the allocator's locks or its latency.
 // For them qdtg_unique_points_noalloc() computes what the batch path's first
 // stage computes (reference builder.hxx:356-390: the points sorted by
@@ -12,10 +11,13 @@
 // caller passes its own device input and output.
 //
 // The array lives on every GPU that loads the library until the process
-// exits. All calls share it, and it keeps the last call's contents; the
-// kernel initialises everything it reads, so nothing needs clearing between
-// calls. Calls that overlap on the GPU (on different streams, or from
-// different host threads) race on the array: serialise them.
+// exits. All calls share it, and it keeps the last call's contents: the
+// kernel initialises everything it reads, and the host sets the two status
+// words to a value no kernel writes before each launch, so a launch that did
+// not run can never pass for a result. Calls that overlap on the GPU (on
+// different streams, or from different host threads) race on the array:
+// serialise them. The call reads its status back into host memory and waits
+// for its stream before it returns.
 #include <cstdint>
 #include <mutex>
 
@@ -234,16 +236,36 @@ QDT_API qdt_status qdtg_unique_points_noalloc(const qdt_vec2d* d_pts, size_t n, 
         scratch = g_na_ptr[dev];
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
+    if (s)
+    {
+        // the array's address above is the current device's: a stream of
+        // another device would run the kernel on that device's array
+        int sdev = -1;
+        if (cudaStreamGetDevice(s, &sdev) != cudaSuccess || sdev != dev)
+        {
+            cudaGetLastError();
+            return QDT_ERR_INTERNAL;
+        }
+    }
+    uint32_t* d_status = reinterpret_cast<uint32_t*>(scratch + (size_t)40 * kNoAllocMaxPoints);
+    // status words to 0xFFFFFFFF, which the kernel never writes: a launch
+    // that did not run leaves them there instead of the last call's result
+    if (cudaMemsetAsync(d_status, 0xFF, 2 * sizeof(uint32_t), s) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return QDT_ERR_INTERNAL;
+    }
     k_unique_noalloc<<<1, kNoAllocThreads, 0, s>>>(reinterpret_cast<const double2*>(d_pts), (int)n, scratch, d_rep);
-    uint32_t st[2] = { 0, 0 };
-    if (cudaMemcpyAsync(st, scratch + (size_t)40 * kNoAllocMaxPoints, sizeof st, cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
+    if (cudaGetLastError() != cudaSuccess) return QDT_ERR_INTERNAL;
+    uint32_t st[2] = { 0xFFFFFFFFu, 0xFFFFFFFFu };
+    if (cudaMemcpyAsync(st, d_status, sizeof st, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
     {
         cudaGetLastError();
         return QDT_ERR_INTERNAL;
     }
-    if (st[0]) return QDT_ERR_NOT_FINITE;
+    if (st[0] == 1u) return QDT_ERR_NOT_FINITE;
+    if (st[0] != 0u || st[1] > (uint32_t)n) return QDT_ERR_INTERNAL;
     *unique_points = st[1];
     return QDT_OK;
 }

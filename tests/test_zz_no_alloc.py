@@ -1,10 +1,12 @@
 """qdtg_unique_points_noalloc: the batch path's first stage for callers that
-cannot allocate device memory (graph capture that must not allocate, hosts
-that own every allocation, real-time loops). Called through the C ABI on
+cannot allocate device memory (hosts that own every allocation, real-time
+loops that may not take the allocator's locks). Called through the C ABI on
 device arrays the test owns, twice in a row on different inputs, and
 compared with the representatives and distinct count that the regular entry
 point (qdt_execute) produces for the same points. Integer outputs: the
-comparison is exact.
+comparison is exact. One more case runs on a stream of its own and checks
+that a warm call changes neither torch's allocation count nor the device's
+free memory.
 
 This file is collected last on purpose, so a run that stops at the first
 failure has run every other test before it.
@@ -29,12 +31,13 @@ def regular(lib, pts):
         return t.rep_array(), t.run_info()["unique_points"]
 
 
-def noalloc(lib, torch, pts):
+def noalloc(lib, torch, pts, stream=None):
     d = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
     rep = torch.full((pts.shape[0],), 0xFFFFFFFF, dtype=torch.int64, device="cuda").to(torch.int32)
     torch.cuda.synchronize()
     uniq = ctypes.c_size_t(12345)
-    st = lib.qdtg_unique_points_noalloc(d.data_ptr(), pts.shape[0], rep.data_ptr(), ctypes.byref(uniq), None)
+    handle = None if stream is None else stream.cuda_stream
+    st = lib.qdtg_unique_points_noalloc(d.data_ptr(), pts.shape[0], rep.data_ptr(), ctypes.byref(uniq), handle)
     torch.cuda.synchronize()
     return st, rep.cpu().numpy().astype(np.uint32), uniq.value
 
@@ -71,3 +74,32 @@ def test_noalloc_limits_and_errors():
     uniq = ctypes.c_size_t(7)
     assert lib.qdtg_unique_points_noalloc(None, 0, None, ctypes.byref(uniq), None) == Q.QDT_OK and uniq.value == 0
     assert lib.qdtg_unique_points_noalloc(None, 5, None, ctypes.byref(uniq), None) == Q.QDT_ERR_NULL_ARGUMENT
+
+
+def test_noalloc_on_own_stream_allocates_nothing():
+    torch = pytest.importorskip("torch")
+    lib = G.load()
+    pts = W.lattice_with_duplicates(120, 0.05, 4)
+    want_rep, want_uniq = regular(lib, pts)
+    stream = torch.cuda.Stream()
+    d = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+    rep = torch.zeros(pts.shape[0], dtype=torch.int32, device="cuda")
+    uniq = ctypes.c_size_t(0)
+    torch.cuda.synchronize()
+    # warm call: the first call on a device looks up the array's address
+    assert lib.qdtg_unique_points_noalloc(d.data_ptr(), pts.shape[0], rep.data_ptr(), ctypes.byref(uniq),
+                                          stream.cuda_stream) == Q.QDT_OK
+    torch.cuda.synchronize()
+    rep.fill_(-1)
+    torch.cuda.synchronize()
+    used = torch.cuda.memory_allocated()
+    free_before, _ = torch.cuda.mem_get_info()
+    uniq = ctypes.c_size_t(0)
+    st = lib.qdtg_unique_points_noalloc(d.data_ptr(), pts.shape[0], rep.data_ptr(), ctypes.byref(uniq),
+                                        stream.cuda_stream)
+    free_after, _ = torch.cuda.mem_get_info()
+    assert st == Q.QDT_OK
+    assert torch.cuda.memory_allocated() == used
+    assert free_after == free_before
+    assert uniq.value == want_uniq
+    assert np.array_equal(rep.cpu().numpy().astype(np.uint32), want_rep)
