@@ -69,6 +69,14 @@ QDT_API int qdtg_set_graphs(qdt_t* ptr, int use_graphs);
    same. Returns 1, or 0 for a NULL context or no usable GPU. */
 QDT_API int qdtg_set_split_tail(qdt_t* ptr, int on);
 
+/* Before each upper depth of the build, the records near that depth's
+   seams are pulled into L2. With on != 0 (the default) that selection and
+   prefetch runs on a second stream beside the previous depth's merges when
+   no other engine is running a call, else in line. The prefetch reads only
+   record numbers it selected and never writes a record, so the result is
+   the same either way. Returns 1, or 0 for a NULL context or no usable GPU. */
+QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
+
 /* Caps the device bytes of the context's workspace (0: no cap, the
    default). A batch call whose workspace would exceed the cap returns
    QDT_ERR_OUT_OF_MEMORY and leaves the context empty, as when cudaMalloc

@@ -26,7 +26,7 @@ GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_windo
                "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints", "qdtg_set_workspace_limit", "qdtg_context_workspace_bytes",
-               "qdtg_set_split_tail",
+               "qdtg_set_split_tail", "qdtg_set_side_prefetch",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -91,6 +91,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_graphs.restype = ctypes.c_int
     lib.qdtg_set_split_tail.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_split_tail.restype = ctypes.c_int
+    lib.qdtg_set_side_prefetch.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_side_prefetch.restype = ctypes.c_int
     lib.qdtg_set_workspace_limit.argtypes = [P, ctypes.c_size_t]
     lib.qdtg_set_workspace_limit.restype = ctypes.c_int
     lib.qdtg_context_workspace_bytes.argtypes = [P]
@@ -219,6 +221,9 @@ class Triangulation(qdt_api.Context):
 
     def set_split_tail(self, on: bool) -> bool:
         return self.lib.qdtg_set_split_tail(self.ptr, int(bool(on))) == 1
+
+    def set_side_prefetch(self, on: bool) -> bool:
+        return self.lib.qdtg_set_side_prefetch(self.ptr, int(bool(on))) == 1
 
     def set_workspace_limit(self, nbytes: int) -> bool:
         """Caps the device workspace (0: no cap); calls that need more

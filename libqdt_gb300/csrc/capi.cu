@@ -562,6 +562,15 @@ QDT_API int qdtg_set_split_tail(qdt_t* ptr, int on)
     return 1;
 }
 
+QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on)
+{
+    Context* c = ctx(ptr);
+    if (!c) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_side_prefetch(on != 0);
+    return 1;
+}
+
 QDT_API int qdtg_set_workspace_limit(qdt_t* ptr, size_t bytes)
 {
     Context* c = ctx(ptr);

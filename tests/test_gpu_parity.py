@@ -185,6 +185,31 @@ def test_split_tail_same_result(lib):
                 assert min(launches[True]) < min(launches[False]), (p.shape, launches)
 
 
+def test_side_prefetch_same_result(lib):
+    """The seam prefetch of the next depth runs on a side stream while the
+    current depth's merges edit the records it scans (a read-only hint: it
+    selects record numbers below the pool size and never writes a record).
+    On and off give bit-identical triangle and representative arrays, and on
+    the 1M uniform workload the reference's digest."""
+    spec = next(s for s in _DIGESTS if s["name"] == "uniform_1m")
+    inputs = [("uniform_1m", C.make_large(spec)), ("lattice", W.lattice_with_duplicates(400, 0.01, 91)),
+              ("gauss", W.gaussian_mixture(300000, 64, 92)), ("circle", W.unit_circle(70000, 93))]
+    for name, p in inputs:
+        got = {}
+        for side in (False, True, False, True):
+            with G.Triangulation(lib) as t:
+                assert t.set_side_prefetch(side)
+                assert t.execute(p) == 0
+                got.setdefault(side, []).append((t.triangles_array().copy(), t.rep_array().copy()))
+        ref_tris, ref_rep = got[False][0]
+        for side in (False, True):
+            for tris, rep in got[side]:
+                assert np.array_equal(tris, ref_tris), (name, side)
+                assert np.array_equal(rep, ref_rep), (name, side)
+        if name == "uniform_1m":
+            assert _digest(O.canonical(ref_tris).astype(np.int64)) == spec["serial"]["tri_digest"]
+
+
 def test_merge_window_same_result(lib):
     """The warp merges' candidate window (1 or 2) is a schedule: the same
     triangulation either way; the automatic choice takes 1 on lattice-like
