@@ -113,7 +113,49 @@ def large_specs():
     specs.append({"name": "gauss_4m", "gen": "gauss", "n": 4000000, "seed": 11})
     specs.append({"name": "circle_100k", "gen": "circle", "n": 100000, "seed": 13})
     specs.append({"name": "line_1m", "gen": "line", "n": 1000000, "seed": 17})
+    specs.append({"name": "uniform_16m", "gen": "uniform", "n": 1 << 24, "seed": 3})
     return specs
+
+
+# The many-set workload at its stated size: 4,096 sets, sizes log-uniform in
+# [16, 65,536], square or disk, 10 % snapped to a 256 x 256 grid.
+CONFIG_B = {"count": 4096, "lo": 16, "hi": 65536, "seed": 23}
+
+
+def config_b_sets():
+    return W.many_sets(**CONFIG_B)
+
+
+def canonical_small(tris: np.ndarray) -> np.ndarray:
+    """The canonical form of oracle.canonical (each triangle rotated to its
+    smallest index, rows sorted) for indices below 2^16, by one sort of
+    packed 48-bit keys: the same array, faster on the 4,096 sets."""
+    t = np.asarray(tris, dtype=np.int64).reshape(-1, 3)
+    if t.shape[0] == 0:
+        return t
+    assert t.max() < (1 << 16) and t.min() >= 0
+    k = np.argmin(t, axis=1)
+    idx = (k[:, None] + np.arange(3)[None, :]) % 3
+    r = np.take_along_axis(t, idx, axis=1).astype(np.uint64)
+    key = np.sort((r[:, 0] << np.uint64(32)) | (r[:, 1] << np.uint64(16)) | r[:, 2])
+    out = np.empty((key.shape[0], 3), dtype=np.int64)
+    out[:, 0] = (key >> np.uint64(32)).astype(np.int64)
+    out[:, 1] = ((key >> np.uint64(16)) & np.uint64(0xFFFF)).astype(np.int64)
+    out[:, 2] = (key & np.uint64(0xFFFF)).astype(np.int64)
+    return out
+
+
+def digest64(a: np.ndarray) -> int:
+    """The first 8 bytes of the SHA-256 of an array's bytes, as an integer."""
+    import hashlib
+    return int.from_bytes(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest()[:8], "little")
+
+
+def set_record(status: int, tris: np.ndarray, used: np.ndarray):
+    """(status, triangle count, digest of the canonical triangles, digest of
+    the used-point flags) of one set: what the config-B fixture keeps."""
+    ct = canonical_small(tris)
+    return int(status), int(ct.shape[0]), digest64(ct), digest64(np.asarray(used, dtype=np.uint8))
 
 
 def make_large(spec) -> np.ndarray:

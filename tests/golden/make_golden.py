@@ -13,7 +13,11 @@ writes:
 * small_cases.npz -- points, canonical triangles and used flags of small
   structured and random cases (full arrays);
 * digests.json    -- for the large workloads: counts and SHA-256 digests of
-  the canonical triangle list and of the used flags.
+  the canonical triangle list and of the used flags;
+* config_b.npz    -- the many-set workload at its stated size (4,096 sets):
+  per set the status, the triangle count and 64-bit digests of the
+  canonical triangles and of the used flags (`--config-b-only` makes this
+  file alone).
 
 The canonical form is the reference harness's (qdt_verify.cpp:408-427).
 Nothing at test time reads the reference; the tests read only these files.
@@ -77,6 +81,10 @@ def main():
         return 1
     lib = Q.load(O.REF_LIB_PATH)
     mesh_only = "--mesh-only" in sys.argv   # regenerate mesh_cases.npz alone
+    if "--config-b-only" in sys.argv:
+        return make_config_b(lib)
+    if "--large-only" in sys.argv:
+        return make_large(lib)
 
     small = {}
     for name, pts in ([] if mesh_only else C.small_cases()):
@@ -123,6 +131,28 @@ def main():
     if mesh_only:
         return 0
 
+    make_large(lib)
+    return make_config_b(lib)
+
+
+def make_config_b(lib):
+    """Every set of the many-set workload through the reference's
+    qdt_execute, one call per set (the serial batch path)."""
+    t0 = time.time()
+    sets = C.config_b_sets()
+    rec = np.zeros((len(sets), 4), dtype=np.uint64)
+    sizes = np.array([p.shape[0] for p in sets], dtype=np.int64)
+    for i, p in enumerate(sets):
+        st, tris, used = run_ref(lib, p, False)
+        r = C.set_record(st, tris, used)
+        rec[i] = [np.uint64(r[0] & 0xFFFFFFFFFFFFFFFF), r[1], r[2], r[3]]
+    np.savez_compressed(os.path.join(HERE, "config_b.npz"), sizes=sizes, status=rec[:, 0].astype(np.int64),
+                        ntri=rec[:, 1].astype(np.int64), tri_digest=rec[:, 2], used_digest=rec[:, 3])
+    print("config B: %d sets, %d points, %.1fs" % (len(sets), int(sizes.sum()), time.time() - t0))
+    return 0
+
+
+def make_large(lib):
     out = {"canonical_form": "qdt_verify.cpp:408-427", "cases": []}
     for spec in C.large_specs():
         pts = C.make_large(spec)

@@ -6,6 +6,8 @@ empty and tiny sets, duplicates, -0.0, collinear and cocircular sets, a set
 with a NaN among good ones, repeated calls (CUDA graph replay), changing
 shapes and the device-resident entry point. Index outputs: bit-exact.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -13,8 +15,10 @@ import libqdt_gb300 as G
 from libqdt_gb300 import qdt_api as Q
 from libqdt_gb300 import workloads as W
 from oracle import oracle as O
+from tests.golden import cases as C
 
 pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.fixture(scope="module")
@@ -151,3 +155,31 @@ def test_device_resident_batch(lib):
         for i, p in enumerate(sets):
             t = tri[toff[i]: toff[i + 1]]
             assert np.array_equal(O.canonical(t), O.canonical(O.triangulate(p).tris)), i
+
+
+def test_config_b_every_set_equals_reference(lib):
+    """The many-set workload at its stated size -- 4,096 sets, sizes
+    log-uniform in [16, 65,536], square or disk, 10 % snapped to a 256 grid
+    -- in one qdtg_batch_execute call (then a graph replay): every set's
+    status, triangle count and digests of its canonical triangles and
+    used-point flags equal what the reference's qdt_execute gave for that set
+    alone (tests/golden/config_b.npz, made by the reference)."""
+    ref = np.load(os.path.join(GOLDEN, "config_b.npz"))
+    sets = C.config_b_sets()
+    assert np.array_equal(np.array([p.shape[0] for p in sets]), ref["sizes"])
+    with G.Batch(lib) as b:
+        for rep_call in range(2):
+            assert b.execute_sets(sets) == Q.QDT_OK
+            bad = []
+            for i, p in enumerate(sets):
+                st = b.status(i)
+                tris = b.triangles(i)
+                rep = b.rep(i)
+                used = (rep == np.arange(p.shape[0])).astype(np.uint8) if tris.shape[0] else \
+                    np.zeros(p.shape[0], np.uint8)
+                got = C.set_record(st, tris, used)
+                want = (int(ref["status"][i]), int(ref["ntri"][i]), int(ref["tri_digest"][i]),
+                        int(ref["used_digest"][i]))
+                if got != want:
+                    bad.append(i)
+            assert not bad, (rep_call, bad[:10], len(bad))

@@ -61,6 +61,30 @@ def test_alone_vs_in_mix_identical(lib):
             assert np.array_equal(O.canonical(tris), O.canonical(O.triangulate(p).tris)), i
 
 
+def test_large_requests_alone_vs_in_mix_identical(lib):
+    """Requests of 0.5 to 2 million points (the top of the serving
+    workload's size range; uniform, Gaussian mixture and snapped grid)
+    arriving while others run on the large engines, with small requests
+    coalesced beside them: each result equals the same request run alone
+    through qdt_execute."""
+    big = W.request_stream(10, rate_per_s=40.0, lo=500_000, hi=2_000_000, seed=43)
+    small = W.request_stream(40, rate_per_s=160.0, lo=100, hi=20_000, seed=44)
+    reqs = sorted(big + small, key=lambda r: r[0])
+    with S.Server(lib, large_workers=4, small_threshold=65536) as srv:
+        out = S.run_open_loop(srv, reqs, keep_results=True)
+        stats = srv.stats()
+    assert out["completed"] == len(reqs)
+    assert stats["rejected"] == 0
+    assert out["coalesced"] > 0
+    for i, (_, p) in enumerate(reqs):
+        st, tris, rep, uniq = out["results"][i]
+        want = alone(lib, p)
+        assert st == want[0] == Q.QDT_OK, i
+        assert np.array_equal(O.canonical(tris), want[1]), (i, p.shape[0])
+        assert np.array_equal(rep, want[2]), i
+        assert uniq == want[3], i
+
+
 def test_budget_admission_and_queue_limit(lib):
     with S.Server(lib, large_workers=3, small_threshold=1000, batch_max_points=100_000) as srv:
         batch_pool = srv.stats()["resident_bytes"]
