@@ -197,6 +197,25 @@ QDT_API size_t qdtg_download_device_triangles(const qdt_t* ptr, uint32_t* out, s
 QDT_API size_t qdtg_copy_triangles(const qdt_t* ptr, uint32_t* out, size_t cap);
 QDT_API size_t qdtg_copy_rep(const qdt_t* ptr, uint32_t* out, size_t cap);
 
+/* Loads a triangulation made earlier into the context in place of a batch
+   call: pts (n points), rep (the representatives qdtg_copy_rep wrote; NULL
+   when all points are distinct) and tris (ntri triangles as
+   qdtg_copy_triangles wrote them). The context then holds what that batch
+   call left, and insertions, constraints and queries go on from there: a
+   saved triangulation is resumed without triangulating again. Constraints
+   are not part of the saved state. No counterpart in the reference; runs
+   on the host and needs no GPU. The arrays are copied. Checks, in order:
+   NULL context (QDT_ERR_NULL_CONTEXT); n > 1e8 or ntri > 2e8
+   (QDT_ERR_TOO_MANY_POINTS); NULL arrays with n or ntri > 0
+   (QDT_ERR_NULL_ARGUMENT); a NaN or infinite coordinate
+   (QDT_ERR_NOT_FINITE); a representative that is not the lowest index of
+   equal coordinates, a triangle corner out of range or not its own
+   representative, a triangle not strictly counter-clockwise, or a directed
+   edge used twice (QDT_ERR_INVALID_INDEX). Any rejection leaves the
+   context empty. */
+QDT_API qdt_status qdtg_set_triangulation(qdt_t* ptr, const qdt_vec2d* pts, size_t n, const uint32_t* rep,
+    const uint32_t* tris, size_t ntri);
+
 /* The CUDA stream (a cudaStream_t) on which the context's GPU work runs;
    NULL before the context's first batch call. Lets a caller order its own
    work or time the calls with CUDA events on that stream. */

@@ -26,7 +26,7 @@ GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_windo
                "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints", "qdtg_set_workspace_limit", "qdtg_context_workspace_bytes",
-               "qdtg_set_split_tail", "qdtg_set_side_prefetch",
+               "qdtg_set_split_tail", "qdtg_set_side_prefetch", "qdtg_set_triangulation",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -91,6 +91,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_graphs.restype = ctypes.c_int
     lib.qdtg_set_split_tail.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_split_tail.restype = ctypes.c_int
+    lib.qdtg_set_triangulation.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_size_t]
+    lib.qdtg_set_triangulation.restype = ctypes.c_int
     lib.qdtg_set_side_prefetch.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_side_prefetch.restype = ctypes.c_int
     lib.qdtg_set_workspace_limit.argtypes = [P, ctypes.c_size_t]
@@ -221,6 +224,17 @@ class Triangulation(qdt_api.Context):
 
     def set_split_tail(self, on: bool) -> bool:
         return self.lib.qdtg_set_split_tail(self.ptr, int(bool(on))) == 1
+
+    def set_triangulation(self, pts, tris, rep=None) -> int:
+        """Loads a triangulation made earlier (points, triangles and
+        representatives as triangles_array / rep_array gave them) in place of
+        a batch call; works without a GPU."""
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 2)
+        t = np.ascontiguousarray(tris, dtype=np.uint32).reshape(-1, 3)
+        r = None if rep is None else np.ascontiguousarray(rep, dtype=np.uint32)
+        return self.lib.qdtg_set_triangulation(self.ptr, p.ctypes.data if p.size else None, p.shape[0],
+                                               None if r is None else r.ctypes.data,
+                                               t.ctypes.data if t.size else None, t.shape[0])
 
     def set_side_prefetch(self, on: bool) -> bool:
         return self.lib.qdtg_set_side_prefetch(self.ptr, int(bool(on))) == 1

@@ -1,14 +1,17 @@
 // The C interface (include/qdt.h, include/qdt_gpu.h): input checks, status
 // codes, reset-on-failure, queries. Mirrors the reference shim
 // (libqdt/qdt.cpp) function by function; no C++ exception crosses it.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include <cuda_runtime.h>
 
 #include "common.cuh"
 #include "context.hpp"
+#include "predicates.cuh"
 #include "qdt.h"
 #include "qdt_gpu.h"
 
@@ -663,6 +666,80 @@ QDT_API size_t qdtg_copy_rep(const qdt_t* ptr, uint32_t* out, size_t cap)
     const size_t k = std::min(cap, c->rep.size());
     std::copy(c->rep.data(), c->rep.data() + k, out);
     return k;
+}
+
+// No counterpart in the reference: loads a saved triangulation (qdt_gpu.h).
+QDT_API qdt_status qdtg_set_triangulation(qdt_t* ptr, const qdt_vec2d* pts, size_t n, const uint32_t* rep,
+    const uint32_t* tris, size_t ntri)
+{
+    Context* c = ctx(ptr);
+    if (!c) return QDT_ERR_NULL_CONTEXT;
+    try
+    {
+        c->reset();
+        if (n > qdtg::kMaxPoints || ntri > 2 * qdtg::kMaxPoints) return QDT_ERR_TOO_MANY_POINTS;
+        if ((n && !pts) || (ntri && !tris)) return QDT_ERR_NULL_ARGUMENT;
+        for (size_t i = 0; i < n; ++i)
+            if (!point_ok(pts[i].x, pts[i].y)) return QDT_ERR_NOT_FINITE;
+        // representatives: the lowest index with the same coordinates (-0.0
+        // equals +0.0)
+        size_t uniq = 0;
+        {
+            auto bits = [](double v) {
+                uint64_t b;
+                v = v == 0.0 ? 0.0 : v;
+                std::memcpy(&b, &v, sizeof b);
+                return b;
+            };
+            std::vector<std::pair<std::pair<uint64_t, uint64_t>, uint32_t>> order(n);
+            for (size_t i = 0; i < n; ++i) order[i] = { { bits(pts[i].x), bits(pts[i].y) }, (uint32_t)i };
+            std::sort(order.begin(), order.end());
+            for (size_t k = 0; k < n;)
+            {
+                size_t j = k;
+                const uint32_t lowest = order[k].second;
+                for (; j < n && order[j].first == order[k].first; ++j)
+                {
+                    const uint32_t i = order[j].second;
+                    if ((rep ? rep[i] : i) != lowest) return QDT_ERR_INVALID_INDEX;
+                }
+                ++uniq;
+                k = j;
+            }
+        }
+        // triangles: representatives as corners, strictly counter-clockwise,
+        // every directed edge once
+        std::vector<uint64_t> edges;
+        edges.reserve(3 * ntri);
+        for (size_t t = 0; t < ntri; ++t)
+        {
+            const uint32_t* T = tris + 3 * t;
+            for (int k = 0; k < 3; ++k)
+                if (T[k] >= n || (rep && rep[T[k]] != T[k])) return QDT_ERR_INVALID_INDEX;
+            const qdt_vec2d &a = pts[T[0]], &b = pts[T[1]], &d = pts[T[2]];
+            if (qdtg::orient2d_sign(a.x, a.y, b.x, b.y, d.x, d.y) <= 0) return QDT_ERR_INVALID_INDEX;
+            for (int k = 0; k < 3; ++k) edges.push_back(((uint64_t)T[k] << 32) | T[(k + 1) % 3]);
+        }
+        std::sort(edges.begin(), edges.end());
+        if (std::adjacent_find(edges.begin(), edges.end()) != edges.end()) return QDT_ERR_INVALID_INDEX;
+        c->points.resize(2 * n);
+        for (size_t i = 0; i < n; ++i)
+        {
+            c->points[2 * i] = pts[i].x;
+            c->points[2 * i + 1] = pts[i].y;
+        }
+        c->rep.resize(n);
+        for (size_t i = 0; i < n; ++i) c->rep[i] = rep ? rep[i] : (uint32_t)i;
+        c->tris.assign(tris, tris + 3 * ntri);
+        c->unique_points = uniq;
+        return QDT_OK;
+    }
+    catch (...)
+    {
+        const qdt_status st = status_from_current_exception();
+        c->reset_release();
+        return st;
+    }
 }
 
 QDT_API int qdtg_last_cuda_error(const qdt_t* ptr)

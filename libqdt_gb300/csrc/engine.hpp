@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstddef>
 #include <cstdint>
+#include <cstdlib>
 #include <memory>
 #include <new>
 #include <map>
@@ -21,11 +22,15 @@ namespace qdtg {
 
 // Allocator for host buffers that the GPU copies to and from: page-locked
 // memory (cudaHostAlloc), and default-initialisation so that resize() does not
-// clear memory that a copy overwrites anyway.
+// clear memory that a copy overwrites anyway. Where page-locked memory cannot
+// be had (no usable GPU: a context that only holds a loaded triangulation and
+// edits it on the host) it falls back to ordinary heap memory; a 64-byte
+// header in front of each block records which.
 template <class T>
 struct PinnedAllocator
 {
     using value_type = T;
+    static constexpr size_t kHeader = 64;
     PinnedAllocator() = default;
     template <class U>
     PinnedAllocator(const PinnedAllocator<U>&) noexcept
@@ -33,18 +38,26 @@ struct PinnedAllocator
     }
     T* allocate(size_t n)
     {
-        void* p = nullptr;
-        if (n == 0) n = 1;
-        if (cudaHostAlloc(&p, n * sizeof(T), cudaHostAllocPortable) != cudaSuccess)
+        if (n > (SIZE_MAX - kHeader) / sizeof(T)) throw std::bad_alloc();
+        const size_t bytes = kHeader + (n ? n : 1) * sizeof(T);
+        void*        p = nullptr;
+        unsigned char kind = 1;
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess)
         {
             cudaGetLastError();
-            throw std::bad_alloc();
+            p = std::aligned_alloc(kHeader, (bytes + kHeader - 1) / kHeader * kHeader);
+            if (!p) throw std::bad_alloc();
+            kind = 2;
         }
-        return static_cast<T*>(p);
+        *static_cast<unsigned char*>(p) = kind;
+        return reinterpret_cast<T*>(static_cast<unsigned char*>(p) + kHeader);
     }
     void deallocate(T* p, size_t) noexcept
     {
-        if (p) cudaFreeHost(p);
+        if (!p) return;
+        unsigned char* base = reinterpret_cast<unsigned char*>(p) - kHeader;
+        if (*base == 1) cudaFreeHost(base);
+        else std::free(base);
     }
     template <class U>
     void construct(U* p) noexcept

@@ -3,27 +3,37 @@
 //
 // The batch engine leaves triangles, representatives and points in the
 // context. The first insertion or constraint builds a half-edge mesh from
-// them (reference GuibasStolfiDwyer_Wrapper.cpp:99-202); afterwards the mesh
-// and the context's triangle list are kept in step. The algorithms are the
-// published ones the reference uses, written here from their definitions:
+// them (on the GPU when the engine still holds the result, k_mesh.cu; else
+// here); afterwards the mesh and the context's triangle list change
+// together. Both operations produce the constrained Delaunay triangulation
+// of the new input directly, each with a published method:
 //
-// * insertion (Wrapper.cpp:531-876): locate the point by a visibility walk
-//   with a scan as fallback; split the triangle it lies in (or the two
-//   triangles of the edge it lies on, or join it to the visible hull edges
-//   when it lies outside); restore the Delaunay property with Lawson flips
-//   that never flip a constrained edge;
-// * constraints (Wrapper.cpp:878-1285): trace the segment through the mesh,
-//   reject it when it crosses a constrained edge or passes through a vertex,
-//   flip the crossed edges away (Sloan 1993), mark the new edge constrained,
-//   and re-legalise with Lawson flips.
+// * insertion: the Bowyer-Watson cavity -- the triangles whose circumcircle
+//   holds the new point strictly, grown from the triangle(s) that contain
+//   it across unconstrained edges (and, for a point beyond the hull, the
+//   hull edges it sees) -- replaced by the fan of the point over the
+//   cavity's border. A constrained edge the point lies on is split into two
+//   constrained edges.
+// * constraints: the channel of triangles the open segment crosses (it is
+//   refused when it runs through a vertex or crosses a constrained edge) is
+//   removed and the two pseudo-polygons on either side of the segment are
+//   triangulated by Anglada's recursion (1997): the base edge takes the
+//   polygon vertex whose circle with it holds no other polygon vertex, and
+//   the two sub-polygons it leaves are filled the same way.
 //
-// All geometric decisions use the exact predicates of predicates.cuh.
+// The results are the ones the reference's insertion and constraint calls
+// produce (GuibasStolfiDwyer_Wrapper.cpp:531-876 and :878-1285: statuses,
+// indices, and in general position the same triangles, the constrained
+// Delaunay triangulation being unique there). An edit gives back exactly
+// the triangle slots and half-edges it frees and appends the rest, so the
+// triangle list stays dense and every half-edge of the mesh is in use. All
+// geometric decisions use the exact predicates of predicates.cuh.
 #include <algorithm>
 #include <atomic>
 #include <climits>
 #include <cmath>
-#include <deque>
-#include <unordered_map>
+#include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "context.hpp"
@@ -51,15 +61,16 @@ struct SeedGrid
 
 struct Mesh
 {
-    MeshVec<MV>      v;
-    MeshVec<HE>      h;
-    std::vector<int> free_h;
-    MeshVec<int>     o2l;    // point index -> mesh vertex, -1 when none
-    std::vector<int> t2h;    // triangle -> one of its half-edges
-    SeedGrid         grid;
-    int              last = 0;
-    uint64_t         id = next_id();   // identifies this mesh to the device mirror
-    uint64_t         version = 0;      // bumped by every call that may change the mesh
+    MeshVec<MV>           v;
+    MeshVec<HE>           h;        // every entry in use
+    MeshVec<int>          o2l;      // point index -> mesh vertex, -1 when none
+    std::vector<int>      t2h;      // triangle -> one of its half-edges
+    std::vector<uint32_t> mark;     // per triangle: the stamp of the last edit that took it
+    uint32_t              stamp = 0;
+    SeedGrid              grid;
+    int                   last = 0;   // a half-edge near the last edit: the next walk's default start
+    uint64_t              id = next_id();   // identifies this mesh to the device mirror
+    uint64_t              version = 0;      // bumped by every call that may change the mesh
 
     static uint64_t next_id()
     {
@@ -72,25 +83,219 @@ void mesh_destroy(Mesh* m) noexcept { delete m; }
 
 namespace {
 
-inline int orient(const Mesh& M, int a, int b, double px, double py)
+// ---- mesh navigation -------------------------------------------------------
+
+inline int nxt(const Mesh& M, int e) { return M.h[e].next; }
+inline int prv(const Mesh& M, int e) { return M.h[M.h[e].next].next; }
+inline int dst(const Mesh& M, int e) { return M.h[M.h[e].next].org; }
+
+// orientation of p against the half-edge e (> 0: p on its triangle's side)
+inline int side(const Mesh& M, int e, double px, double py)
 {
-    const MV &A = M.v[a], &B = M.v[b];
+    const MV &A = M.v[M.h[e].org], &B = M.v[dst(M, e)];
     return orient2d_sign(A.x, A.y, B.x, B.y, px, py);
 }
-inline int orient3(const Mesh& M, int a, int b, int c) { return orient(M, a, b, M.v[c].x, M.v[c].y); }
-inline int incircle4(const Mesh& M, int a, int b, int c, int d)
+inline int orient3(const Mesh& M, int a, int b, int c)
+{
+    const MV &A = M.v[a], &B = M.v[b], &C = M.v[c];
+    return orient2d_sign(A.x, A.y, B.x, B.y, C.x, C.y);
+}
+// > 0 when d lies strictly inside the circle through a, b, c (counter-clockwise)
+inline int circle4(const Mesh& M, int a, int b, int c, int d)
 {
     const MV &A = M.v[a], &B = M.v[b], &C = M.v[c], &D = M.v[d];
     return incircle_sign(A.x, A.y, B.x, B.y, C.x, C.y, D.x, D.y);
 }
+// > 0 when (px, py) lies strictly inside the circumcircle of triangle slot t
+inline int circle_holds(const Mesh& M, int t, double px, double py)
+{
+    const int  e = M.t2h[t];
+    const MV&  A = M.v[M.h[e].org];
+    const MV&  B = M.v[dst(M, e)];
+    const MV&  C = M.v[M.h[prv(M, e)].org];
+    return incircle_sign(A.x, A.y, B.x, B.y, C.x, C.y, px, py);
+}
 
-// Builds the half-edge mesh from the context's triangles (Wrapper.cpp:99-202).
+// Visits the outgoing half-edges of vertex x, one per triangle around it,
+// counter-clockwise; around a hull vertex the visit starts at the clockwise-
+// most one, so the open fan is covered once. f returns true to stop; the
+// result says whether it did.
+template <class F>
+bool around(const Mesh& M, int x, F&& f)
+{
+    int s = M.v[x].he;
+    if (s < 0) return false;
+    const size_t cap = M.h.size() + 1;
+    size_t       n = 0;
+    // clockwise neighbour of k: the half-edge after its twin
+    for (int k = s;;)
+    {
+        const int t = M.h[k].twin;
+        if (t < 0)
+        {
+            s = k;
+            break;
+        }
+        k = M.h[t].next;
+        if (k == s || ++n > cap) break;
+    }
+    n = 0;
+    for (int k = s;;)
+    {
+        if (f(k)) return true;
+        const int t = M.h[prv(M, k)].twin;   // counter-clockwise neighbour
+        if (t < 0 || t == s || ++n > cap) return false;
+        k = t;
+    }
+}
+
+// A half-edge of the edge u-w (u -> w, or w -> u where only that side has a
+// triangle), or -1.
+int edge_between(const Mesh& M, int u, int w)
+{
+    int found = -1;
+    around(M, u, [&](int k) {
+        if (dst(M, k) == w) found = k;
+        else if (M.h[prv(M, k)].org == w) found = prv(M, k);
+        return found >= 0;
+    });
+    return found;
+}
+
+void set_constrained(Mesh& M, int e)
+{
+    M.h[e].cons = 1;
+    if (M.h[e].twin >= 0) M.h[M.h[e].twin].cons = 1;
+}
+
+// the hull half-edge after / before hull half-edge e (interior on its left)
+int hull_after(const Mesh& M, int e)
+{
+    int k = nxt(M, e);   // out of e's end; turn clockwise until the hull
+    for (size_t n = 0; M.h[k].twin >= 0 && n <= M.h.size(); ++n) k = M.h[M.h[k].twin].next;
+    return k;
+}
+int hull_before(const Mesh& M, int e)
+{
+    int k = prv(M, e);   // into e's start; turn counter-clockwise until the hull
+    for (size_t n = 0; M.h[k].twin >= 0 && n <= M.h.size(); ++n) k = prv(M, M.h[k].twin);
+    return k;
+}
+
+// A fresh stamp for marking the triangles one edit takes.
+uint32_t new_stamp(Mesh& M, size_t ntri)
+{
+    if (M.mark.size() < ntri) M.mark.resize(ntri, 0);
+    if (++M.stamp == 0)
+    {
+        std::fill(M.mark.begin(), M.mark.end(), 0u);
+        M.stamp = 1;
+    }
+    return M.stamp;
+}
+
+// ---- writing triangles -----------------------------------------------------
+
+// Triangle slots and half-edge ids for the triangles an edit makes: first
+// the ones it removed, then new ones at the end of the arrays.
+struct Reuse
+{
+    std::vector<int> slots, hes;
+    size_t           ns = 0, nh = 0;
+
+    size_t slot(const Context& c) { return ns < slots.size() ? (size_t)slots[ns++] : c.ntris(); }
+    int    he(Mesh& M)
+    {
+        if (nh < hes.size()) return hes[nh++];
+        M.h.push_back(HE{ -1, -1, -1, -1, 0 });
+        return (int)M.h.size() - 1;
+    }
+    bool all_used() const { return ns == slots.size() && nh == hes.size(); }
+};
+
+// Triangle slot t (t == ntris() appends) becomes e0 -> e1 -> e2 with origins
+// a, b, d, counter-clockwise; twins and constraint flags are left to the
+// caller.
+void put_triangle(Context& c, Mesh& M, size_t t, int e0, int e1, int e2, int a, int b, int d)
+{
+    const int ti = (int)t;
+    M.h[e0].org = a, M.h[e0].next = e1, M.h[e0].tri = ti;
+    M.h[e1].org = b, M.h[e1].next = e2, M.h[e1].tri = ti;
+    M.h[e2].org = d, M.h[e2].next = e0, M.h[e2].tri = ti;
+    const uint32_t o[3] = { M.v[a].orig, M.v[b].orig, M.v[d].orig };
+    if (t == c.ntris())
+    {
+        c.tris.insert(c.tris.end(), o, o + 3);
+        M.t2h.push_back(e0);
+    }
+    else
+    {
+        std::copy(o, o + 3, c.tris.begin() + 3 * t);
+        M.t2h[t] = e0;
+    }
+}
+
+// Gives the triangles in `slots` to r: their slots and half-edges.
+void reuse_triangles(const Mesh& M, const std::vector<int>& slots, Reuse& r)
+{
+    r.slots = slots;
+    r.hes.clear();
+    for (int t : slots)
+    {
+        const int e = M.t2h[t];
+        r.hes.push_back(e);
+        r.hes.push_back(nxt(M, e));
+        r.hes.push_back(prv(M, e));
+    }
+}
+
+inline uint64_t edge_key(int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
+
+// ---- point location --------------------------------------------------------
+
+// A half-edge of a triangle that contains (x, y) (border included), or -1
+// with *seen set to a hull half-edge whose outer side the point lies
+// strictly on. The walk of mesh_walk.cuh first; a scan of every triangle,
+// then of every hull edge, when it gives up.
+int find_point(const Mesh& M, int start, double x, double y, int* seen, size_t* steps)
+{
+    *seen = -1;
+    const int nv = (int)M.v.size(), nh = (int)M.h.size();
+    if (nh == 0) return -1;
+    if (start < 0 || start >= nh) start = (M.last >= 0 && M.last < nh) ? M.last : 0;
+    int             n = 0;
+    const int       cap = (int)std::min<size_t>(M.t2h.size() + 16, (size_t)INT_MAX);
+    const LocResult r = walk(M.v.data(), M.h.data(), nv, nh, start, x, y, cap, &n);
+    if (steps) *steps = (size_t)n;
+    if (r.where == kLocInside) return r.he;
+    if (r.where == kLocOutside)
+    {
+        *seen = r.he;
+        return -1;
+    }
+    for (size_t t = 0; t < M.t2h.size(); ++t)
+    {
+        const int e = M.t2h[t];
+        if (side(M, e, x, y) >= 0 && side(M, nxt(M, e), x, y) >= 0 && side(M, prv(M, e), x, y) >= 0) return e;
+    }
+    for (int e = 0; e < nh; ++e)
+        if (M.h[e].twin < 0 && side(M, e, x, y) < 0)
+        {
+            *seen = e;
+            return -1;
+        }
+    return -1;
+}
+
+// Builds the half-edge mesh from the context's triangles (what the reference
+// builds at Wrapper.cpp:99-202): vertices numbered by first appearance in the
+// triangle list, three half-edges per triangle, twins matched through the
+// outgoing half-edges grouped by origin.
 void build_mesh(Context& c, Mesh& M)
 {
     const size_t T = c.ntris();
     M.v.clear();
     M.h.clear();
-    M.free_h.clear();
     M.t2h.clear();
     M.last = 0;
     M.o2l.assign(c.npoints(), -1);
@@ -151,7 +356,6 @@ bool build_mesh_on_device(Context& c, Mesh& M)
     if (!c.mesh_on_gpu || !c.engine) return false;
     const size_t T = c.ntris();
     if (c.engine->build_mesh(c.npoints(), T, M.o2l, M.v, M.h) != 0) return false;
-    M.free_h.clear();
     M.last = 0;
     M.t2h.reserve(T + std::max<size_t>(T / 8, 1024));
     M.t2h.resize(T);
@@ -194,107 +398,6 @@ Mesh& ensure_mesh(Context& c)
         c.mesh = m;
     }
     return *c.mesh;
-}
-
-int alloc_he(Mesh& M)
-{
-    if (!M.free_h.empty())
-    {
-        const int k = M.free_h.back();
-        M.free_h.pop_back();
-        return k;
-    }
-    M.h.push_back(HE{ -1, -1, -1, -1, false });
-    return (int)M.h.size() - 1;
-}
-
-void free_he(Mesh& M, int k)
-{
-    M.h[k] = HE{ -1, -1, -1, -1, false };
-    M.free_h.push_back(k);
-}
-
-size_t add_tri(Context& c, Mesh& M, int a, int b, int d, int h0)
-{
-    const size_t t = c.ntris();
-    c.tris.push_back(M.v[a].orig);
-    c.tris.push_back(M.v[b].orig);
-    c.tris.push_back(M.v[d].orig);
-    M.t2h.push_back(h0);
-    return t;
-}
-
-// removes triangle idx by moving the last triangle into its slot
-void remove_tri(Context& c, Mesh& M, size_t idx)
-{
-    const size_t last = c.ntris() - 1;
-    if (idx != last)
-    {
-        for (int i = 0; i < 3; ++i) c.tris[3 * idx + i] = c.tris[3 * last + i];
-        const int moved = M.t2h[last];
-        M.t2h[idx] = moved;
-        int e = moved;
-        do
-        {
-            M.h[e].tri = (int)idx;
-            e = M.h[e].next;
-        } while (e != moved);
-    }
-    c.tris.resize(3 * last);
-    M.t2h.pop_back();
-}
-
-// Visibility walk (Wrapper.cpp:423-486), scan as fallback (:491-521).
-// Returns a half-edge of the triangle containing p (border included), or -1
-// with *hull set to a hull half-edge that p sees. The walk starts at the
-// half-edge `start` when it is alive, else at the last insertion.
-int locate(const Mesh& M, size_t ntri, double px, double py, int* hull, int start = -1, size_t* steps = nullptr)
-{
-    *hull = -1;
-    if (M.h.empty() || ntri == 0) return -1;
-    int h = (start >= 0 && start < (int)M.h.size() && M.h[start].org >= 0) ? start : M.last;
-    if (h < 0 || h >= (int)M.h.size() || M.h[h].org < 0)
-    {
-        h = 0;
-        while (h < (int)M.h.size() && M.h[h].org < 0) ++h;
-        if (h >= (int)M.h.size()) return -1;
-    }
-    for (size_t step = 0; step < ntri + 16; ++step)
-    {
-        if (steps) *steps = step + 1;
-        const int h0 = h, h1 = M.h[h0].next, h2 = M.h[h1].next;
-        if (M.h[h2].next != h0) break;
-        const int o0 = orient(M, M.h[h0].org, M.h[h1].org, px, py);
-        const int o1 = orient(M, M.h[h1].org, M.h[h2].org, px, py);
-        const int o2 = orient(M, M.h[h2].org, M.h[h0].org, px, py);
-        if (o0 >= 0 && o1 >= 0 && o2 >= 0) return h0;
-        const int cross = o0 < 0 ? h0 : (o1 < 0 ? h1 : h2);
-        const int tw = M.h[cross].twin;
-        if (tw < 0)
-        {
-            *hull = cross;
-            return -1;
-        }
-        h = tw;
-    }
-    for (size_t t = 0; t < M.t2h.size(); ++t)
-    {
-        const int h0 = M.t2h[t], h1 = M.h[h0].next, h2 = M.h[h1].next;
-        if (orient(M, M.h[h0].org, M.h[h1].org, px, py) >= 0 && orient(M, M.h[h1].org, M.h[h2].org, px, py) >= 0 &&
-            orient(M, M.h[h2].org, M.h[h0].org, px, py) >= 0)
-            return h0;
-    }
-    for (size_t i = 0; i < M.h.size(); ++i)
-    {
-        const HE& e = M.h[i];
-        if (e.org < 0 || e.twin >= 0) continue;
-        if (orient(M, e.org, M.h[e.next].org, px, py) < 0)
-        {
-            *hull = (int)i;
-            return -1;
-        }
-    }
-    return -1;
 }
 
 size_t seed_cell(const SeedGrid& g, double x, double y)
@@ -396,175 +499,130 @@ void seed_account(Mesh& M, size_t steps)
     if (M.grid.walked > M.v.size() / 32 + 64) seed_build(M);
 }
 
-// Flips the diagonal h (Wrapper.cpp:942-1009). Before: triangles
-// (a, b, c) with h = a->b and (b, a, d) with twin = b->a. After: (d, c, a)
-// and (c, d, b). Refused unless both new triangles are strictly
-// counter-clockwise, or when h is constrained or on the hull.
-bool flip(Context& c, Mesh& M, int h)
-{
-    const int tw = M.h[h].twin;
-    if (tw < 0 || M.h[h].cons) return false;
-    const int hn = M.h[h].next, hp = M.h[hn].next;
-    const int tn = M.h[tw].next, tp = M.h[tn].next;
-    const int a = M.h[h].org, b = M.h[hn].org, cc = M.h[hp].org, d = M.h[tp].org;
-    if (orient3(M, d, cc, a) <= 0 || orient3(M, cc, d, b) <= 0) return false;
-    // triangle 1: h = d->c, hp = c->a, tn = a->d
-    M.h[h].org = d;
-    M.h[h].next = hp;
-    M.h[hp].next = tn;
-    M.h[tn].next = h;
-    // triangle 2: tw = c->d, tp = d->b, hn = b->c
-    M.h[tw].org = cc;
-    M.h[tw].next = tp;
-    M.h[tp].next = hn;
-    M.h[hn].next = tw;
-    const int t1 = M.h[h].tri, t2 = M.h[tw].tri;
-    M.h[tn].tri = t1;
-    M.h[hn].tri = t2;
-    c.tris[3 * t1 + 0] = M.v[d].orig;
-    c.tris[3 * t1 + 1] = M.v[cc].orig;
-    c.tris[3 * t1 + 2] = M.v[a].orig;
-    c.tris[3 * t2 + 0] = M.v[cc].orig;
-    c.tris[3 * t2 + 1] = M.v[d].orig;
-    c.tris[3 * t2 + 2] = M.v[b].orig;
-    M.t2h[t1] = h;
-    M.t2h[t2] = tw;
-    M.v[a].he = tn;
-    M.v[b].he = hn;
-    M.v[cc].he = hp;
-    M.v[d].he = h;
-    return true;
-}
-
-// Calls f(h) for every half-edge h leaving x until f returns true
-// (Wrapper.cpp:885-923): counter-clockwise from the stored one, then
-// clockwise for hull vertices.
-template <class F>
-void for_each_out(const Mesh& M, int x, F&& f)
-{
-    const int h0 = M.v[x].he;
-    if (h0 < 0) return;
-    const size_t limit = M.h.size();
-    size_t       steps = 0;
-    int          h = h0;
-    for (;;)
-    {
-        if (f(h)) return;
-        if (++steps > limit) return;
-        const int prev = M.h[M.h[h].next].next;
-        const int tw = M.h[prev].twin;
-        if (tw < 0) break;
-        if (tw == h0) return;
-        h = tw;
-    }
-    h = h0;
-    for (;;)
-    {
-        const int tw = M.h[h].twin;
-        if (tw < 0) return;
-        h = M.h[tw].next;
-        if (h == h0) return;
-        if (f(h)) return;
-        if (++steps > limit) return;
-    }
-}
-
-int find_he(const Mesh& M, int u, int w)
-{
-    int found = -1;
-    for_each_out(M, u, [&](int h) {
-        if (M.h[M.h[h].next].org == w)
-        {
-            found = h;
-            return true;
-        }
-        return false;
-    });
-    return found;
-}
-
-void mark_cons(Mesh& M, int h)
-{
-    M.h[h].cons = true;
-    if (M.h[h].twin >= 0) M.h[M.h[h].twin].cons = true;
-}
-
-bool segments_cross(const Mesh& M, int a, int b, int c, int d)
-{
-    const int o1 = orient3(M, a, b, c), o2 = orient3(M, a, b, d);
-    const int o3 = orient3(M, c, d, a), o4 = orient3(M, c, d, b);
-    return ((o1 > 0 && o2 < 0) || (o1 < 0 && o2 > 0)) && ((o3 > 0 && o4 < 0) || (o3 < 0 && o4 > 0));
-}
-
-// Lists the edges the open segment u-w crosses, each as the half-edge from
-// the vertex right of u->w to the one on its left (Wrapper.cpp:1050-1106).
-int trace(const Mesh& M, size_t ntri, int u, int w, std::vector<int>& crossed)
-{
-    int  start = -1;
-    bool blocked = false;
-    for_each_out(M, u, [&](int h) {
-        const int hn = M.h[h].next;
-        const int y = M.h[hn].org, z = M.h[M.h[hn].next].org;
-        const int oy = orient3(M, u, y, w), oz = orient3(M, u, z, w);
-        if (oy > 0 && oz < 0)
-        {
-            start = hn;
-            return true;
-        }
-        if ((oy == 0 && same_direction(M.v[u], M.v[y], M.v[w])) ||
-            (oz == 0 && same_direction(M.v[u], M.v[z], M.v[w])))
-        {
-            blocked = true;
-            return true;
-        }
-        return false;
-    });
-    if (blocked) return QDT_ERR_THROUGH_POINT;
-    if (start < 0) return QDT_ERR_INTERNAL;
-    int e = start;
-    for (size_t guard = 0; guard <= ntri; ++guard)
-    {
-        if (M.h[e].cons) return QDT_ERR_CROSSES_CONSTRAINT;
-        crossed.push_back(e);
-        const int tw = M.h[e].twin;
-        if (tw < 0) return QDT_ERR_INTERNAL;
-        const int a = M.h[tw].next, b = M.h[a].next;
-        const int x = M.h[b].org;
-        if (x == w) return QDT_OK;
-        const int o = orient3(M, u, w, x);
-        if (o == 0) return QDT_ERR_THROUGH_POINT;
-        e = o > 0 ? a : b;
-    }
-    return QDT_ERR_INTERNAL;
-}
-
-// Lawson's flips over a stack of half-edges (Wrapper.cpp:1111-1142).
-void legalize(Context& c, Mesh& M, std::vector<int>& stack)
-{
-    while (!stack.empty())
-    {
-        const int h = stack.back();
-        stack.pop_back();
-        if (M.h[h].org < 0) continue;
-        const int tw = M.h[h].twin;
-        if (tw < 0 || M.h[h].cons) continue;
-        const int hn = M.h[h].next, hp = M.h[hn].next;
-        const int tn = M.h[tw].next, tp = M.h[tn].next;
-        const int a = M.h[h].org, b = M.h[hn].org, cc = M.h[hp].org, d = M.h[tp].org;
-        if (incircle4(M, a, b, cc, d) <= 0) continue;
-        if (!flip(c, M, h)) continue;
-        stack.push_back(hp);
-        stack.push_back(hn);
-        stack.push_back(tn);
-        stack.push_back(tp);
-    }
-}
-
 int insert_by_rebuild(Context& c, double x, double y)
 {
     c.points.push_back(x);
     c.points.push_back(y);
     return rebuild_from_points(c);
+}
+
+// One border edge of an insertion cavity: the new triangle (a, b, p) takes
+// it, and its half-edge a -> b faces `ext` (-1 on the hull).
+struct Border
+{
+    int a, b, ext, cons;
+};
+
+// The Bowyer-Watson cavity of (x, y): `in` is a half-edge of a triangle that
+// contains the point (or -1 with `seen` a hull edge the point sees). The
+// cavity grows from the triangle(s) that contain the point (or from the
+// triangles behind the hull edges it sees) into neighbours whose
+// circumcircle holds the point strictly, crossing an edge only outward (the
+// point strictly on the near side) and never a constrained edge. Its border
+// must be strictly visible from the point; a triangle whose border edge is
+// not (one hidden behind a constrained edge) is excluded and the cavity is
+// grown again. Fills the cavity's triangle slots, its border in a fixed
+// order, and the constrained edge the point splits (split_a, split_b; -1
+// when none). false when no star-shaped cavity is found, which exact
+// predicates rule out; the mesh is not changed here.
+bool insertion_cavity(Context& c, Mesh& M, int in, int seen, double x, double y, std::vector<int>& cav,
+    std::vector<Border>& border, int& split_a, int& split_b)
+{
+    std::vector<int> sees;   // hull edges the point sees from outside, in hull order
+    if (in < 0)
+    {
+        // they form one chain: listed from its first edge in hull order
+        auto sees_it = [&](int e) { return side(M, e, x, y) < 0; };
+        int  first = seen;
+        for (int e = hull_before(M, seen); e != seen && sees_it(e); e = hull_before(M, e)) first = e;
+        sees.push_back(first);
+        for (int e = hull_after(M, first); e != first && sees_it(e); e = hull_after(M, e)) sees.push_back(e);
+    }
+    std::vector<int> excluded;
+    auto             is_excluded = [&](int t) { return std::find(excluded.begin(), excluded.end(), t) != excluded.end(); };
+    for (int round = 0; round < 256; ++round)
+    {
+        cav.clear();
+        border.clear();
+        split_a = split_b = -1;
+        const uint32_t stamp = new_stamp(M, c.ntris());
+        auto           taken = [&](int t) { return M.mark[t] == stamp; };
+        auto           take = [&](int t) {
+            M.mark[t] = stamp;
+            cav.push_back(t);
+        };
+        size_t seeds = 0;
+        if (in >= 0)
+        {
+            take(M.h[in].tri);
+            // a point on an edge takes the triangle across it too, across a
+            // constrained edge as well (which it splits)
+            for (int k = 0, e = in; k < 3; ++k, e = nxt(M, e))
+                if (side(M, e, x, y) == 0)
+                {
+                    const int tw = M.h[e].twin;
+                    if (tw >= 0 && !taken(M.h[tw].tri)) take(M.h[tw].tri);
+                    if (M.h[e].cons)
+                    {
+                        split_a = M.h[e].org;
+                        split_b = dst(M, e);
+                    }
+                }
+            seeds = cav.size();
+        }
+        else
+            for (int e : sees)
+            {
+                const int t = M.h[e].tri;
+                if (!taken(t) && !is_excluded(t) && circle_holds(M, t, x, y) > 0) take(t);
+            }
+        for (size_t i = 0; i < cav.size(); ++i)
+        {
+            const int e0 = M.t2h[cav[i]];
+            for (int k = 0, e = e0; k < 3; ++k, e = nxt(M, e))
+            {
+                const int tw = M.h[e].twin;
+                if (tw < 0 || M.h[e].cons) continue;
+                const int t = M.h[tw].tri;
+                if (taken(t) || is_excluded(t) || side(M, e, x, y) <= 0) continue;
+                if (circle_holds(M, t, x, y) > 0) take(t);
+            }
+        }
+        // the border: edges of cavity triangles whose other side stays, in
+        // the order the triangles joined; then the seen hull edges whose
+        // triangle stays, crossed from outside
+        int hidden = -1;
+        for (size_t i = 0; i < cav.size() && hidden < 0; ++i)
+        {
+            const int e0 = M.t2h[cav[i]];
+            for (int k = 0, e = e0; k < 3; ++k, e = nxt(M, e))
+            {
+                const int tw = M.h[e].twin;
+                if (tw >= 0 && taken(M.h[tw].tri)) continue;
+                const int s = side(M, e, x, y);
+                if (s > 0)
+                    border.push_back(Border{ M.h[e].org, dst(M, e), tw, M.h[e].cons });
+                else if (tw < 0 && ((s == 0 && i < seeds) ||
+                                    (s < 0 && std::find(sees.begin(), sees.end(), e) != sees.end())))
+                    continue;   // a hull edge the point splits, or one it sees: inside the cavity
+                else
+                {
+                    hidden = cav[i];
+                    break;
+                }
+            }
+        }
+        if (hidden >= 0)
+        {
+            if (in >= 0 && std::find(cav.begin(), cav.begin() + seeds, hidden) != cav.begin() + seeds) return false;
+            excluded.push_back(hidden);
+            continue;
+        }
+        for (int e : sees)
+            if (!taken(M.h[e].tri)) border.push_back(Border{ dst(M, e), M.h[e].org, e, M.h[e].cons });
+        return !border.empty();
+    }
+    return false;
 }
 
 }  // namespace
@@ -576,18 +634,16 @@ int mesh_insert_point(Context& c, double x, double y, bool, int hint)
     if (M.h.empty()) return insert_by_rebuild(c, x, y);
     ++M.version;
 
-    int    hull = -1;
+    int    seen = -1;
     size_t steps = 0;
     if (hint < 0) hint = seed_start(M, x, y);
-    int h_start = locate(M, c.ntris(), x, y, &hull, hint, &steps);
+    int in = find_point(M, hint, x, y, &seen, &steps);
     seed_account(M, steps);
-    if (h_start < 0 && hull < 0) return insert_by_rebuild(c, x, y);
-    const bool outside = h_start < 0;
-    if (!outside)
+    if (in < 0 && seen < 0) return insert_by_rebuild(c, x, y);
+    if (in >= 0)
     {
-        // a vertex equal to p is a corner of the triangle that contains it
-        int e = h_start;
-        do
+        // a point equal to a vertex is a corner of the triangle it was found in
+        for (int k = 0, e = in; k < 3; ++k, e = nxt(M, e))
         {
             const MV& q = M.v[M.h[e].org];
             if (q.x == x && q.y == y)
@@ -597,214 +653,241 @@ int mesh_insert_point(Context& c, double x, double y, bool, int hint)
                 c.rep.push_back(q.orig);
                 return QDT_OK;
             }
-            e = M.h[e].next;
-        } while (e != h_start);
-        // start from the canonical containing triangle (the smaller index of
-        // the two when p lies on an edge), so that the result does not depend
-        // on where the walk began
-        const LocResult cl =
-            classify(M.v.data(), M.h.data(), (int)M.v.size(), (int)M.h.size(), h_start, x, y, INT_MAX);
+        }
+        // the cavity grows from the canonical containing triangle (the
+        // smaller one when the point is on an edge): the triangle order of
+        // the result does not depend on where the walk began
+        const LocResult cl = classify(M.v.data(), M.h.data(), (int)M.v.size(), (int)M.h.size(), in, x, y, INT_MAX);
         if ((cl.where == kLocInside || cl.where == kLocEdge) && cl.tri >= 0 && cl.tri < (int)M.t2h.size())
-            h_start = M.t2h[cl.tri];
+            in = M.t2h[cl.tri];
     }
-    M.last = outside ? hull : h_start;
 
+    std::vector<int>    cav;
+    std::vector<Border> border;
+    int                 split_a = -1, split_b = -1;
+    if (!insertion_cavity(c, M, in, seen, x, y, cav, border, split_a, split_b)) return QDT_ERR_INTERNAL;
+
+    // the new vertex
     const uint32_t id = (uint32_t)c.npoints();
     c.points.push_back(x);
     c.points.push_back(y);
     c.rep.push_back(id);
     ++c.unique_points;
-    const int nv = (int)M.v.size();
+    const int p = (int)M.v.size();
     M.v.push_back(MV{ x, y, id, -1 });
     if (M.o2l.size() <= id) M.o2l.resize(id + 1, -1);
-    M.o2l[id] = nv;
-    if (!M.grid.cell.empty()) M.grid.cell[seed_cell(M.grid, x, y)] = nv;
+    M.o2l[id] = p;
+    if (!M.grid.cell.empty()) M.grid.cell[seed_cell(M.grid, x, y)] = p;
 
-    // visible hull edges (outside case)
-    std::vector<int> visible;
-    if (outside)
+    // the fan of p over the border; spokes b -> p and p -> b pair up by b
+    Reuse r;
+    reuse_triangles(M, cav, r);
+    std::vector<std::pair<int, int>> into, out;   // (b, b -> p), (a, p -> a)
+    into.reserve(border.size());
+    out.reserve(border.size());
+    int first_spoke = -1;
+    for (const Border& q : border)
     {
-        auto vis = [&](int e) { return orient(M, M.h[e].org, M.h[M.h[e].next].org, x, y) < 0; };
-        auto next_hull = [&](int e) {
-            int k = M.h[e].next;
-            while (M.h[k].twin >= 0) k = M.h[M.h[k].twin].next;
-            return k;
-        };
-        auto prev_hull = [&](int e) {
-            int k = M.h[M.h[e].next].next;
-            while (M.h[k].twin >= 0)
-            {
-                const int t = M.h[k].twin;
-                k = M.h[M.h[t].next].next;
-            }
-            return k;
-        };
-        // the visible hull edges form one chain; list it from its first edge
-        // (in hull order), whichever edge the walk found
-        int s = hull;
-        for (int e = prev_hull(hull); e != hull && vis(e); e = prev_hull(e)) s = e;
-        visible.push_back(s);
-        for (int e = next_hull(s); e != s && vis(e); e = next_hull(e)) visible.push_back(e);
-        M.last = s;
+        const size_t t = r.slot(c);
+        const int    e0 = r.he(M), e1 = r.he(M), e2 = r.he(M);
+        put_triangle(c, M, t, e0, e1, e2, q.a, q.b, p);
+        M.h[e0].twin = q.ext;
+        M.h[e0].cons = q.cons;
+        if (q.ext >= 0) M.h[q.ext].twin = e0;
+        M.h[e1].twin = M.h[e2].twin = -1;
+        M.h[e1].cons = M.h[e2].cons = 0;
+        M.v[q.a].he = e0;
+        into.emplace_back(q.b, e1);
+        out.emplace_back(q.a, e2);
+        if (first_spoke < 0) first_spoke = e2;
     }
-
-    // the cavity: the triangle that contains p, and the one across the edge p
-    // lies on, if any
-    std::vector<int> cav_he, cav_tri;
-    auto             in_cav = [&](int t) { return std::find(cav_tri.begin(), cav_tri.end(), t) != cav_tri.end(); };
-    int              split_a = -1, split_b = -1;
-    if (!outside)
+    if (!r.all_used()) return QDT_ERR_INTERNAL;
+    std::sort(into.begin(), into.end());
+    std::sort(out.begin(), out.end());
+    for (size_t i = 0, j = 0; i < into.size() && j < out.size();)
     {
-        auto add = [&](int e) {
-            const int t = M.h[e].tri;
-            if (t >= 0 && !in_cav(t))
-            {
-                cav_tri.push_back(t);
-                cav_he.push_back(e);
-            }
-        };
-        add(h_start);
-        int e = h_start;
-        do
+        if (into[i].first < out[j].first) ++i;
+        else if (out[j].first < into[i].first) ++j;
+        else
         {
-            const int en = M.h[e].next;
-            if (orient(M, M.h[e].org, M.h[en].org, x, y) == 0)
-            {
-                if (M.h[e].twin >= 0) add(M.h[e].twin);
-                if (M.h[e].cons)
-                {
-                    split_a = M.h[e].org;
-                    split_b = M.h[en].org;
-                }
-            }
-            e = en;
-        } while (e != h_start);
-    }
-
-    struct Bnd
-    {
-        int  a, b, ext;
-        bool cons;
-    };
-    std::vector<Bnd> bnd;
-    for (int h0 : cav_he)
-    {
-        int e = h0;
-        do
-        {
-            const int tw = M.h[e].twin;
-            const int twt = tw >= 0 ? M.h[tw].tri : -1;
-            if (!(twt >= 0 && in_cav(twt)))
-            {
-                const int a = M.h[e].org, b = M.h[M.h[e].next].org;
-                if (tw >= 0 || orient(M, a, b, x, y) > 0) bnd.push_back(Bnd{ a, b, tw, M.h[e].cons != 0 });
-            }
-            e = M.h[e].next;
-        } while (e != h0);
-    }
-    for (int e : visible)
-    {
-        const int t = M.h[e].tri;
-        if (t >= 0 && in_cav(t)) continue;
-        const int a = M.h[e].org, b = M.h[M.h[e].next].org;
-        bnd.push_back(Bnd{ b, a, e, M.h[e].cons != 0 });
-    }
-
-    std::sort(cav_tri.rbegin(), cav_tri.rend());
-    for (int t : cav_tri) remove_tri(c, M, (size_t)t);
-    for (int h0 : cav_he)
-    {
-        int e = h0;
-        do
-        {
-            const int en = M.h[e].next;
-            free_he(M, e);
-            e = en;
-        } while (e != h0);
-    }
-
-    struct NT
-    {
-        int h0, h1, h2;
-    };
-    std::vector<NT> nts;
-    for (const Bnd& q : bnd)
-    {
-        const int h0 = alloc_he(M), h1 = alloc_he(M), h2 = alloc_he(M);
-        M.h[h0] = HE{ q.a, q.ext, h1, -1, q.cons };
-        M.h[h1] = HE{ q.b, -1, h2, -1, false };
-        M.h[h2] = HE{ nv, -1, h0, -1, false };
-        if (q.ext >= 0)
-        {
-            M.h[q.ext].twin = h0;
-            M.h[q.ext].cons = q.cons;
-        }
-        const int t = (int)add_tri(c, M, q.a, q.b, nv, h0);
-        M.h[h0].tri = M.h[h1].tri = M.h[h2].tri = t;
-        nts.push_back(NT{ h0, h1, h2 });
-    }
-    if (nts.empty())
-    {
-        // cannot happen with exact predicates; start over from the points
-        c.points.resize(c.points.size() - 2);
-        c.rep.pop_back();
-        return insert_by_rebuild(c, x, y);
-    }
-    {
-        std::unordered_map<int, int> by_b, by_a;   // b -> (b->p), a -> (p->a)
-        for (const NT& t : nts)
-        {
-            by_b[M.h[t.h1].org] = t.h1;
-            by_a[M.h[t.h0].org] = t.h2;
-        }
-        for (const auto& kv : by_b)
-        {
-            const auto it = by_a.find(kv.first);
-            if (it != by_a.end())
-            {
-                M.h[kv.second].twin = it->second;
-                M.h[it->second].twin = kv.second;
-            }
+            M.h[into[i].second].twin = out[j].second;
+            M.h[out[j].second].twin = into[i].second;
+            ++i, ++j;
         }
     }
-    M.v[nv].he = nts[0].h2;
-    M.last = nts[0].h0;
-    for (size_t i = 0; i < nts.size(); ++i)
-    {
-        M.v[bnd[i].a].he = nts[i].h0;
-        M.v[bnd[i].b].he = nts[i].h1;
-    }
+    M.v[p].he = first_spoke;
+    // the two halves of a split constrained edge stay constrained
     if (split_a >= 0)
-    {
-        for (size_t i = 0; i < nts.size(); ++i)
-        {
-            if (bnd[i].b == split_a || bnd[i].b == split_b) mark_cons(M, nts[i].h1);
-            if (bnd[i].a == split_a || bnd[i].a == split_b) mark_cons(M, nts[i].h2);
-        }
-    }
-
-    // Lawson flips around p: h0 of every new triangle faces p
-    std::vector<int> pending;
-    for (const NT& t : nts) pending.push_back(t.h0);
-    while (!pending.empty())
-    {
-        const int h = pending.back();
-        pending.pop_back();
-        const int tw = M.h[h].twin;
-        if (tw < 0 || M.h[h].cons) continue;
-        const int hn = M.h[h].next, hp = M.h[hn].next;
-        if (M.h[hp].org != nv) continue;
-        const int tn = M.h[tw].next, tp = M.h[tn].next;
-        const int a = M.h[h].org, b = M.h[hn].org, d = M.h[tp].org;
-        if (incircle4(M, a, b, nv, d) <= 0) continue;
-        if (flip(c, M, h))
-        {
-            pending.push_back(tn);
-            pending.push_back(tp);
-        }
-    }
+        for (const auto& s : into)
+            if (s.first == split_a || s.first == split_b) set_constrained(M, s.second);
+    M.last = M.t2h[M.h[first_spoke].tri];
     return QDT_OK;
 }
+
+namespace {
+
+// The triangles the open segment u-w crosses, from u to w, and the vertices
+// on either side of it in the same order.
+struct Channel
+{
+    std::vector<int> tris;
+    std::vector<int> left, right;
+};
+
+// Finds the triangle at u that the segment leaves through, then crosses one
+// edge at a time to w. QDT_OK, QDT_ERR_THROUGH_POINT (a vertex on the open
+// segment), QDT_ERR_CROSSES_CONSTRAINT, or QDT_ERR_INTERNAL on a broken
+// mesh; whichever comes first along the segment decides.
+int open_channel(const Mesh& M, int u, int w, Channel& ch)
+{
+    int  leave = -1;
+    bool through = false;
+    around(M, u, [&](int k) {
+        // triangle (u, x, y): the segment leaves through x-y when it runs
+        // strictly between u->x and u->y
+        const int x = dst(M, k), y = M.h[prv(M, k)].org;
+        const int ox = orient3(M, u, x, w), oy = orient3(M, u, y, w);
+        if (ox > 0 && oy < 0) leave = nxt(M, k);
+        else if ((ox == 0 && same_direction(M.v[u], M.v[x], M.v[w])) ||
+                 (oy == 0 && same_direction(M.v[u], M.v[y], M.v[w])))
+            through = true;
+        return leave >= 0 || through;
+    });
+    if (through) return QDT_ERR_THROUGH_POINT;
+    if (leave < 0) return QDT_ERR_INTERNAL;
+    ch.tris.push_back(M.h[leave].tri);
+    // `leave` runs from the vertex right of u->w to the one on its left
+    for (size_t n = 0; n <= M.t2h.size(); ++n)
+    {
+        if (M.h[leave].cons) return QDT_ERR_CROSSES_CONSTRAINT;
+        const int rv = M.h[leave].org, lv = dst(M, leave);
+        if (ch.right.empty() || ch.right.back() != rv) ch.right.push_back(rv);
+        if (ch.left.empty() || ch.left.back() != lv) ch.left.push_back(lv);
+        const int back = M.h[leave].twin;   // lv -> rv in the next triangle
+        if (back < 0) return QDT_ERR_INTERNAL;
+        ch.tris.push_back(M.h[back].tri);
+        const int q = M.h[prv(M, back)].org;
+        if (q == w) return QDT_OK;
+        const int o = orient3(M, u, w, q);
+        if (o == 0) return QDT_ERR_THROUGH_POINT;
+        leave = o > 0 ? nxt(M, back) : prv(M, back);   // rv -> q, or q -> lv
+    }
+    return QDT_ERR_INTERNAL;
+}
+
+struct Tri3
+{
+    int a, b, c;
+};
+
+// Anglada's triangulation of the pseudo-polygon a, b, poly[0], ...,
+// poly[k-1] (counter-clockwise, a -> b its base edge): the base takes the
+// vertex whose circle with it holds no other polygon vertex (the first one
+// on ties), and the polygons on its two sides are filled the same way.
+// false if a triangle would not be strictly counter-clockwise.
+bool fill_polygon(const Mesh& M, int a, int b, const std::vector<int>& poly, std::vector<Tri3>& out)
+{
+    struct Part
+    {
+        int    a, b;
+        size_t lo, hi;
+    };
+    std::vector<Part> todo{ Part{ a, b, 0, poly.size() } };
+    while (!todo.empty())
+    {
+        const Part q = todo.back();
+        todo.pop_back();
+        if (q.lo >= q.hi) continue;
+        size_t best = q.lo;
+        for (size_t i = q.lo + 1; i < q.hi; ++i)
+            if (circle4(M, q.a, q.b, poly[best], poly[i]) > 0) best = i;
+        const int c = poly[best];
+        if (orient3(M, q.a, q.b, c) <= 0) return false;
+        out.push_back(Tri3{ q.a, q.b, c });
+        todo.push_back(Part{ c, q.b, q.lo, best });      // b, poly[lo..best), c
+        todo.push_back(Part{ q.a, c, best + 1, q.hi });  // c, poly(best..hi), a
+    }
+    return true;
+}
+
+// Replaces the channel by the triangulations of its two sides with the
+// edge u-w between them, constrained.
+int fill_channel(Context& c, Mesh& M, int u, int w, const Channel& ch)
+{
+    // left side: u, w, then its vertices back from w; right side: w, u, then
+    // its vertices from u
+    std::vector<int>  lpoly(ch.left.rbegin(), ch.left.rend());
+    std::vector<Tri3> made;
+    if (!fill_polygon(M, u, w, lpoly, made) || !fill_polygon(M, w, u, ch.right, made)) return QDT_ERR_INTERNAL;
+    if (made.size() != ch.tris.size()) return QDT_ERR_INTERNAL;
+
+    // the channel's border half-edges, each with the half-edge facing it
+    // from outside and its constraint flag, keyed as the new triangles run
+    // them
+    const uint32_t stamp = new_stamp(M, c.ntris());
+    for (int t : ch.tris) M.mark[t] = stamp;
+    struct Outer
+    {
+        uint64_t key;
+        int      ext, cons;
+    };
+    std::vector<Outer> outer;
+    for (int t : ch.tris)
+    {
+        const int e0 = M.t2h[t];
+        for (int k = 0, e = e0; k < 3; ++k, e = nxt(M, e))
+        {
+            const int tw = M.h[e].twin;
+            if (tw >= 0 && M.mark[M.h[tw].tri] == stamp) continue;
+            outer.push_back(Outer{ edge_key(M.h[e].org, dst(M, e)), tw, M.h[e].cons });
+        }
+    }
+    std::sort(outer.begin(), outer.end(), [](const Outer& x, const Outer& y) { return x.key < y.key; });
+
+    Reuse r;
+    reuse_triangles(M, ch.tris, r);
+    std::vector<std::pair<uint64_t, int>> fresh;   // (key of a -> b, half-edge)
+    for (const Tri3& q : made)
+    {
+        const size_t t = r.slot(c);
+        const int    e0 = r.he(M), e1 = r.he(M), e2 = r.he(M);
+        put_triangle(c, M, t, e0, e1, e2, q.a, q.b, q.c);
+        const int v3[3] = { q.a, q.b, q.c }, e3[3] = { e0, e1, e2 };
+        for (int k = 0; k < 3; ++k)
+        {
+            fresh.emplace_back(edge_key(v3[k], v3[(k + 1) % 3]), e3[k]);
+            M.h[e3[k]].twin = -1;
+            M.h[e3[k]].cons = 0;
+            M.v[v3[k]].he = e3[k];
+        }
+    }
+    if (!r.all_used()) return QDT_ERR_INTERNAL;
+    std::sort(fresh.begin(), fresh.end());
+    for (const auto& f : fresh)
+    {
+        const uint32_t a = (uint32_t)(f.first >> 32), b = (uint32_t)f.first;
+        const uint64_t rev = edge_key((int)b, (int)a);
+        const auto     in = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(rev, INT_MIN));
+        if (in != fresh.end() && in->first == rev)
+        {
+            M.h[f.second].twin = in->second;   // a diagonal, or the new edge u-w
+            continue;
+        }
+        const auto o = std::lower_bound(outer.begin(), outer.end(), f.first,
+            [](const Outer& x, uint64_t k) { return x.key < k; });
+        if (o == outer.end() || o->key != f.first) return QDT_ERR_INTERNAL;
+        M.h[f.second].twin = o->ext;
+        M.h[f.second].cons = o->cons;
+        if (o->ext >= 0) M.h[o->ext].twin = f.second;
+    }
+    const auto uw = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(edge_key(u, w), INT_MIN));
+    if (uw == fresh.end() || uw->first != edge_key(u, w)) return QDT_ERR_INTERNAL;
+    set_constrained(M, uw->second);
+    M.last = uw->second;
+    return QDT_OK;
+}
+
+}  // namespace
 
 int mesh_insert_constraint(Context& c, size_t v0, size_t v1)
 {
@@ -817,78 +900,16 @@ int mesh_insert_constraint(Context& c, size_t v0, size_t v1)
     const int u = v0 < M.o2l.size() ? M.o2l[v0] : -1;
     const int w = v1 < M.o2l.size() ? M.o2l[v1] : -1;
     if (u < 0 || w < 0) return QDT_ERR_NO_TRIANGLES;
-
-    int e = find_he(M, u, w);
-    if (e < 0) e = find_he(M, w, u);
+    const int e = edge_between(M, u, w);
     if (e >= 0)
     {
-        mark_cons(M, e);
+        set_constrained(M, e);
         return QDT_OK;
     }
-    std::vector<int> crossed;
-    const int        tr = trace(M, c.ntris(), u, w, crossed);
-    if (tr != QDT_OK) return tr;
-
-    std::deque<int>  queue(crossed.begin(), crossed.end());
-    std::vector<int> fresh;
-    size_t           stalled = 0;
-    while (!queue.empty())
-    {
-        const int h = queue.front();
-        queue.pop_front();
-        if (flip(c, M, h))
-        {
-            stalled = 0;
-            const int a = M.h[h].org, b = M.h[M.h[h].next].org;
-            if (segments_cross(M, u, w, a, b)) queue.push_back(h);
-            else fresh.push_back(h);
-        }
-        else
-        {
-            queue.push_back(h);
-            if (++stalled >= queue.size()) break;
-        }
-    }
-    bool ok = false;
-    if (queue.empty())
-    {
-        e = -1;
-        for (int h : fresh)
-        {
-            const int a = M.h[h].org, b = M.h[M.h[h].next].org;
-            if ((a == u && b == w) || (a == w && b == u))
-            {
-                e = h;
-                break;
-            }
-        }
-        if (e < 0) e = find_he(M, u, w);
-        if (e < 0) e = find_he(M, w, u);
-        if (e >= 0)
-        {
-            mark_cons(M, e);
-            ok = true;
-        }
-    }
-    std::vector<int> stack;
-    auto             around = [&](int h) {
-        if (M.h[h].org < 0) return;
-        const int n = M.h[h].next;
-        stack.push_back(h);
-        stack.push_back(n);
-        stack.push_back(M.h[n].next);
-        const int tw = M.h[h].twin;
-        if (tw >= 0)
-        {
-            const int tn = M.h[tw].next;
-            stack.push_back(tn);
-            stack.push_back(M.h[tn].next);
-        }
-    };
-    for (int h : fresh) around(h);
-    for (int h : queue) around(h);
-    legalize(c, M, stack);
-    return ok ? QDT_OK : QDT_ERR_INTERNAL;
+    Channel   ch;
+    const int st = open_channel(M, u, w, ch);
+    if (st != QDT_OK) return st;
+    return fill_channel(c, M, u, w, ch);
 }
 
 int mesh_locate(Context& c, const double* xy, size_t k, int* tri, int* where, int* he)
@@ -926,7 +947,7 @@ int mesh_locate(Context& c, const double* xy, size_t k, int* tri, int* where, in
     {
         if (where[i] != kLocUnresolved) continue;
         int       hull = -1;
-        const int h0 = locate(M, c.ntris(), xy[2 * i], xy[2 * i + 1], &hull);
+        const int h0 = find_point(M, -1, xy[2 * i], xy[2 * i + 1], &hull, nullptr);
         if (h0 >= 0)
         {
             const LocResult r = classify(M.v.data(), M.h.data(), nv, nh, h0, xy[2 * i], xy[2 * i + 1], INT_MAX);

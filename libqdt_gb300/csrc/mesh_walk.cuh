@@ -55,14 +55,16 @@ QDT_HD inline int edge_orient(const MeshVertex* v, const MeshHalfEdge* h, int e,
 // triangle containing the point (border included) with where = kLocInside,
 // or the hull half-edge the point lies beyond with where = kLocOutside, or
 // where = kLocUnresolved after `cap` steps or on an index out of range.
+// *nsteps (when given) receives the triangles visited.
 QDT_HD inline LocResult walk(const MeshVertex* v, const MeshHalfEdge* h, int nv, int nh, int start, double x,
-    double y, int cap)
+    double y, int cap, int* nsteps = nullptr)
 {
     LocResult r{ -1, kLocUnresolved, -1 };
     int       e = start;
     int       entered = -1;   // the edge the walk came in through: the point is strictly left of it
     for (int step = 0; step < cap; ++step)
     {
+        if (nsteps) *nsteps = step + 1;
         if (!he_ok(h, nh, nv, e)) return r;
         const int e1 = h[e].next;
         if (!he_ok(h, nh, nv, e1)) return r;
