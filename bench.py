@@ -524,13 +524,15 @@ def run_stress_leg(lib, args, flush):
         t.set_options(count_filter_failures=True)
         t.execute_device(d_pts.data_ptr(), n)
         info = t.run_info()
+        fstats = t.filter_stats()
         t.set_options(count_filter_failures=False)
         tris = t.download_device_triangles()
         row = {"workload": name, "points": n, "distinct": info["unique_points"], "triangles": int(tris.shape[0]),
                "value": round(n / (statistics.median(ms) / 1e3) / 1e6, 3), "unit": UNIT,
                "ms_per_step": round(statistics.median(ms), 3),
                "exact_per_1000_points": {"orient2d": round(1e3 * info["orient_exact"] / n, 4),
-                                         "incircle": round(1e3 * info["incircle_exact"] / n, 4)}}
+                                         "incircle": round(1e3 * info["incircle_exact"] / n, 4)},
+               "filter_by_stage": stage_rates(fstats, n)}
         if not args.no_check:
             ref = O.triangulate(pts)
             s = ref.stats
@@ -552,6 +554,24 @@ def run_stress_leg(lib, args, flush):
         t.close()
         del d_pts
         torch.cuda.empty_cache()
+    return out
+
+
+def stage_rates(fstats, n):
+    """Per build stage and predicate: the call count, the fraction the float
+    pre-filter left undecided (f32_fail_rate), the fraction the double
+    filter left undecided too (fp64_fail_rate: the exact evaluation ran) and
+    exact evaluations per 1,000 points."""
+    out = {}
+    for stage, preds in fstats.items():
+        row = {}
+        for p, c in preds.items():
+            calls = c["calls"]
+            row[p] = {"calls": calls,
+                      "f32_fail_rate": round(c["f32_undecided"] / calls, 6) if calls else 0.0,
+                      "fp64_fail_rate": round(c["exact"] / calls, 6) if calls else 0.0,
+                      "exact_per_1000_points": round(1e3 * c["exact"] / n, 4)}
+        out[stage] = row
     return out
 
 

@@ -34,6 +34,8 @@ typedef struct qdtg_run_info
     int                device_flags;    /* device status bits; 0 = clean */
     int                kernel_launches; /* kernels the call launched */
     int                merge_window;    /* candidate window of the warp merges (1 or 2; 0 = none ran) */
+    int                wide_exact;      /* 1: a predicate needed the widest exact tier and the build ran
+                                           again with the kernels that have it */
 } qdtg_run_info;
 
 /* Options of a context: count_filter_failures != 0 counts the predicate calls
@@ -170,6 +172,26 @@ QDT_API void qdtg_get_defaults(int* cell_points, int* batch_cell_points, int* si
 /* Fills *info for the last batch call of the context. Returns 1, or 0 when
    ptr or info is NULL. */
 QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info);
+
+/* Predicate statistics of the last batch call, when it counted
+   (qdtg_set_options with count_filter_failures != 0; all zero otherwise),
+   per stage of the build -- [0] leaves (2 or 3 points), [1] merges of a
+   thread per node and shared-memory cells, [2] merges of a warp per node,
+   [3] the extraction's orientation test -- and per predicate ([0]
+   orient2d, [1] in-circle): the calls, the calls the single-precision
+   pre-filter left undecided, and those the double filter left undecided as
+   well (the exact evaluation ran). No counterpart in the reference, which
+   counts nothing. */
+typedef struct qdtg_filter_stats
+{
+    unsigned long long calls[4][2];
+    unsigned long long f32_undecided[4][2];
+    unsigned long long exact[4][2];
+} qdtg_filter_stats;
+
+/* Fills *stats for the last batch call of the context. Returns 1, or 0 when
+   ptr or stats is NULL. */
+QDT_API int qdtg_get_filter_stats(const qdt_t* ptr, qdtg_filter_stats* stats);
 
 /* Batch triangulation of n points that are already in device memory (d_pts,
    16-byte aligned for the fastest path). The work is ordered after the work
@@ -330,6 +352,8 @@ QDT_API int qdtg_batch_set_warp_nodes(qdtg_batch* b, int warp_nodes);
    as qdtg_set_cell_points(). Returns 1, or 0 for a bad value. */
 QDT_API int   qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points);
 QDT_API int   qdtg_batch_get_run_info(const qdtg_batch* b, qdtg_run_info* info);
+/* The same statistics as qdtg_get_filter_stats, for the last call of b. */
+QDT_API int   qdtg_batch_get_filter_stats(const qdtg_batch* b, qdtg_filter_stats* stats);
 QDT_API void* qdtg_batch_stream(const qdtg_batch* b);
 
 /* Pre-allocates the batch's device workspace for up to `points` points in

@@ -26,7 +26,7 @@ GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_windo
                "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints", "qdtg_set_workspace_limit", "qdtg_context_workspace_bytes",
-               "qdtg_set_split_tail", "qdtg_set_side_prefetch", "qdtg_set_triangulation",
+               "qdtg_set_split_tail", "qdtg_get_filter_stats", "qdtg_batch_get_filter_stats", "qdtg_set_side_prefetch", "qdtg_set_triangulation",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -59,6 +59,7 @@ class RunInfo(ctypes.Structure):
         ("device_flags", ctypes.c_int),
         ("kernel_launches", ctypes.c_int),
         ("merge_window", ctypes.c_int),
+        ("wide_exact", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -66,6 +67,19 @@ class RunInfo(ctypes.Structure):
 
 
 _lib = None
+
+
+STAGES = ("leaf", "thread", "warp", "extract")
+
+
+def filter_stats_dict(raw: np.ndarray) -> dict:
+    """qdtg_filter_stats (3 x 4 x 2 unsigned 64-bit) as per-stage dicts of
+    calls, float-undecided and exact counts per predicate."""
+    out = {}
+    for s, name in enumerate(STAGES):
+        out[name] = {p: {"calls": int(raw[0, s, k]), "f32_undecided": int(raw[1, s, k]), "exact": int(raw[2, s, k])}
+                     for k, p in enumerate(("orient2d", "incircle"))}
+    return out
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -89,6 +103,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_merge_window.restype = ctypes.c_int
     lib.qdtg_set_graphs.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_graphs.restype = ctypes.c_int
+    lib.qdtg_get_filter_stats.argtypes = [P, ctypes.c_void_p]
+    lib.qdtg_get_filter_stats.restype = ctypes.c_int
+    lib.qdtg_batch_get_filter_stats.argtypes = [P, ctypes.c_void_p]
+    lib.qdtg_batch_get_filter_stats.restype = ctypes.c_int
     lib.qdtg_set_split_tail.argtypes = [P, ctypes.c_int]
     lib.qdtg_set_split_tail.restype = ctypes.c_int
     lib.qdtg_set_triangulation.argtypes = [P, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
@@ -238,6 +256,13 @@ class Triangulation(qdt_api.Context):
 
     def set_side_prefetch(self, on: bool) -> bool:
         return self.lib.qdtg_set_side_prefetch(self.ptr, int(bool(on))) == 1
+
+    def filter_stats(self) -> dict:
+        """Per-stage predicate statistics of the last batch call (counted
+        when set_options(count_filter_failures=True))."""
+        raw = np.zeros((3, 4, 2), dtype=np.uint64)
+        self.lib.qdtg_get_filter_stats(self.ptr, raw.ctypes.data)
+        return filter_stats_dict(raw)
 
     def set_workspace_limit(self, nbytes: int) -> bool:
         """Caps the device workspace (0: no cap); calls that need more
@@ -411,6 +436,11 @@ class Batch:
 
     def set_cell_points(self, cell_points: int) -> bool:
         return self.lib.qdtg_batch_set_cell_points(self.ptr, int(cell_points)) == 1
+
+    def filter_stats(self) -> dict:
+        raw = np.zeros((3, 4, 2), dtype=np.uint64)
+        self.lib.qdtg_batch_get_filter_stats(self.ptr, raw.ctypes.data)
+        return filter_stats_dict(raw)
 
     def set_warp_nodes(self, nodes: int) -> bool:
         return self.lib.qdtg_batch_set_warp_nodes(self.ptr, int(nodes)) == 1

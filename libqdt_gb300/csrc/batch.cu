@@ -376,8 +376,9 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_height(Rec* __restrict__ R, int
     lo += base;
     hi += base;
     NodeOut* const out = nodes + noff[s];   // heap order: (1 << depth) + index
-    Builder        B{ R, nrec, st, count ? &st->pc : nullptr, -1, -1, false };
     const int      n = hi - lo;
+    Builder        B{ R, nrec, st,
+        pred_stage(st, (LEAF || n <= 3) ? kStageLeaf : (WARP ? kStageWarp : kStageThread), count), -1, -1, false };
     NodeOut        o;
     // height 0 is all leaves, the other heights all merges: two kernels, so
     // that neither carries the other's code
@@ -465,7 +466,7 @@ __global__ void __launch_bounds__(kCellBlockWarps * 32) k_bbuild_cells(Rec* __re
     const long long k = (long long)(g - cell_off[s]);
     int             lo, hi;
     if (!node_range(ms, dc, k, lo, hi) || hi - lo > C) return;
-    build_cell(bcell_smem + w * cell_smem_bytes(C), V, R, base + lo, base + hi, dc, st, count ? &st->pc : nullptr,
+    build_cell(bcell_smem + w * cell_smem_bytes(C), V, R, base + lo, base + hi, dc, st, pred_stage(st, kStageThread, count),
         nodes + noff[s] + (1ll << dc) + k);
 }
 
@@ -480,7 +481,7 @@ __global__ void k_btri_mask(const Rec* __restrict__ R, int nrec, const uint32_t*
         mask[k] = 0;
         return;
     }
-    Builder B{ const_cast<Rec*>(R), nrec, st, count ? &st->pc : nullptr, -1, -1, false };
+    Builder B{ const_cast<Rec*>(R), nrec, st, pred_stage(st, kStageExtract, count), -1, -1, false };
     uint8_t mk = 0;
     if (R[k].org[0] >= 0)
     {
@@ -1063,8 +1064,7 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
     ntri = h_words[1];
     info.ntri = ntri;
     info.device_status = (int)h_status->flags;
-    info.orient_exact = h_status->pc.orient_exact;
-    info.incircle_exact = h_status->pc.incircle_exact;
+    take_pred_stats(info, *h_status);
     info.launches = launch_counter();
     if (timing)
     {
@@ -1334,6 +1334,18 @@ QDT_API int qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points)
     if (!b) return 0;
     if (cell_points != 0 && (cell_points < 4 || cell_points > qdtg::kCellMax)) return 0;
     b->e.cell_points = cell_points;
+    return 1;
+}
+
+namespace qdtg {
+void fill_filter_stats(const RunInfo& r, qdtg_filter_stats* out);
+}
+
+// No counterpart in the reference (qdt_gpu.h).
+QDT_API int qdtg_batch_get_filter_stats(const qdtg_batch* b, qdtg_filter_stats* stats)
+{
+    if (!b || !stats) return 0;
+    qdtg::fill_filter_stats(b->e.info, stats);
     return 1;
 }
 

@@ -521,6 +521,31 @@ QDT_API int qdtg_set_cell_points(qdt_t* ptr, int cell_points)
     return 1;
 }
 
+namespace qdtg {
+// RunInfo's per-stage predicate statistics into the C struct
+void fill_filter_stats(const RunInfo& r, qdtg_filter_stats* out)
+{
+    *out = qdtg_filter_stats{};
+    for (int s = 0; s < kPredStages && s < 4; ++s)
+        for (int k = 0; k < 2; ++k)
+        {
+            out->calls[s][k] = r.stage[s].calls[k];
+            out->f32_undecided[s][k] = r.stage[s].f32_undecided[k];
+            out->exact[s][k] = r.stage[s].exact[k];
+        }
+}
+}  // namespace qdtg
+
+// No counterpart in the reference (qdt_gpu.h).
+QDT_API int qdtg_get_filter_stats(const qdt_t* ptr, qdtg_filter_stats* stats)
+{
+    const Context* c = ctx(ptr);
+    if (!c || !stats) return 0;
+    *stats = qdtg_filter_stats{};
+    if (c->engine) qdtg::fill_filter_stats(c->engine->info(), stats);
+    return 1;
+}
+
 QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
 {
     const Context* c = ctx(ptr);
@@ -544,6 +569,7 @@ QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
     info->device_flags = r.device_status;
     info->kernel_launches = r.launches;
     info->merge_window = r.window;
+    info->wide_exact = r.wide;
     return 1;
 }
 

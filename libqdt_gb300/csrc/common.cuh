@@ -53,18 +53,42 @@ enum StatusBits : unsigned
     ST_BAD_INDEX = 8u,       // an index left its node's range (internal error)
 };
 
-// Filter failures: predicate calls that took the exact integer path.
+// Predicate statistics of one stage of a call ([0] orient2d, [1] in-circle):
+// calls, calls the float pre-filter left undecided, calls the double filter
+// left undecided as well (the exact evaluation ran). They are counted only
+// when the kernel passes its pointer tagged (bit 0 set, pred_stage()).
+// `wide` is set by a predicate that needed the widest exact tier in kernels
+// built without it (predicates.cuh).
 struct PredCounters
 {
-    unsigned long long orient_exact, incircle_exact;
+    unsigned long long calls[2], f32_undecided[2], exact[2];
+    unsigned           wide, pad;
+};
+
+// The stages the statistics are split by: leaves (2-3 points), merges of a
+// thread per node (and shared-memory cells), merges of a warp per node, and
+// the extraction's orientation test.
+enum PredStage : int
+{
+    kStageLeaf = 0,
+    kStageThread = 1,
+    kStageWarp = 2,
+    kStageExtract = 3,
+    kPredStages = 4,
 };
 
 struct DevStatus
 {
     unsigned     flags;
     unsigned     pad;
-    PredCounters pc;
+    PredCounters pc[kPredStages];
 };
+
+// The counters of one stage, tagged when the call counts
+__host__ __device__ inline PredCounters* pred_stage(DevStatus* st, int stage, int count)
+{
+    return reinterpret_cast<PredCounters*>(reinterpret_cast<uintptr_t>(&st->pc[stage]) | (count ? 1u : 0u));
+}
 
 // Depths whose seams (cut coordinates) are recorded during the split, and whose
 // seam records are prefetched into L2 before they merge.

@@ -294,18 +294,23 @@ const uint32_t* Engine::device_rep() const { return w_ ? w_->prep.rep : nullptr;
 
 // frames, split levels, leaf order, build, extraction: the stages after the
 // host has read the distinct-point count m (stream order only, no host work)
-void Engine::post_sync_work(size_t m)
+void Engine::post_sync_work(size_t m, bool wide)
 {
     cudaStream_t  s = stream_;
     PrepBuffers&  p = w_->prep;
     BuildBuffers& b = w_->build;
+    if (wide) cudaMemsetAsync(&p.status->flags, 0, sizeof(unsigned), s);   // the narrow pass's bits
+    // the predicates' counters (the narrow pass's, for a wide one)
+    cudaMemsetAsync(&p.status->pc[0], 0, sizeof(p.status->pc), s);
     launch_frames(p, m, s);
     launch_split(p, (int)m, s);
     launch_finalize(p, (int)m, s);
     mark(4);
-    launch_build(b, (int)m, s);
+    if (wide) wide::launch_build(b, (int)m, s);
+    else narrow::launch_build(b, (int)m, s);
     mark(5);
-    launch_extract(b, (int)m, s);
+    if (wide) wide::launch_extract(b, (int)m, s);
+    else narrow::launch_extract(b, (int)m, s);
 }
 
 void Engine::clear_graphs() noexcept
@@ -429,6 +434,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     // narrow window (builder.cuh, kWinDefault)
     b.window = window_ ? window_ : (16ull * hs->words[2] > (unsigned long long)kTieWindow * m ? 1 : 2);
     info_.window = b.window;
+    info_.wide = 0;
     if (m >= 3)
     {
         // the stages after the count depend only on m and the knobs: one
@@ -437,7 +443,12 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
                                ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
                                ((uint64_t)(p.split_tail ? 1 : 0) << 19) |
                                ((uint64_t)(uint32_t)b.warp_nodes << 20) | ((uint64_t)(b.side ? 1 : 0) << 52);
-        run_graph({ (uint64_t)m, knobs }, [&] { post_sync_work(m); });
+        // a counting call runs the kernels that count every predicate call
+        // (the wide ones) from the start
+        const bool counting = b.count_filter != 0;
+        run_graph({ (uint64_t)m, knobs | (counting ? (1ull << 57) : 0ull) },
+            [&] { post_sync_work(m, counting); });
+        info_.wide = counting ? 1 : 0;
     }
     else
     {
@@ -447,23 +458,41 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
             cudaEventRecord(ev_[5], s);
         }
     }
-    if (timing_) cudaEventRecord(ev_[6], s);
-    cudaMemcpyAsync(&hs->st, p.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(hs->words, w_->words, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-    if (host_io)
+    auto finish = [&] {
+        if (timing_) cudaEventRecord(ev_[6], s);
+        cudaMemcpyAsync(&hs->st, p.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hs->words, w_->words, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (host_io)
+        {
+            // the triangle count is at most 2 m - 5: copy that bound, not a
+            // round trip for the exact count
+            const size_t bound = m >= 3 ? std::min<size_t>(2 * m, host_tri_cap) : 0;
+            if (bound) cudaMemcpyAsync(host_tris, b.tris, 3 * bound * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+            if (n) cudaMemcpyAsync(host_rep, p.rep, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        }
+        if (timing_) cudaEventRecord(ev_[7], s);
+        return cudaStreamSynchronize(s) == cudaSuccess;
+    };
+    if (!finish()) return S_INTERNAL;
+    bool wide = false;
+    for (int sg = 0; sg < kPredStages; ++sg) wide = wide || hs->st.pc[sg].wide;
+    if (m >= 3 && wide && !info_.wide)
     {
-        // the triangle count is at most 2 m - 5: copy that bound, not a
-        // round trip for the exact count
-        const size_t bound = m >= 3 ? std::min<size_t>(2 * m, host_tri_cap) : 0;
-        if (bound) cudaMemcpyAsync(host_tris, b.tris, 3 * bound * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        if (n) cudaMemcpyAsync(host_rep, p.rep, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        // a predicate needed the widest exact tier, which the default
+        // kernels leave out: the stages after the count once more with the
+        // kernels that have it
+        info_.wide = 1;
+        const uint64_t knobs = ((uint64_t)(b.cell_points & 0x7FF) << 4) | ((uint64_t)b.window << 15) |
+                               ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
+                               ((uint64_t)(p.split_tail ? 1 : 0) << 19) |
+                               ((uint64_t)(uint32_t)b.warp_nodes << 20) | ((uint64_t)(b.side ? 1 : 0) << 52) |
+                               (1ull << 57);
+        run_graph({ (uint64_t)m, knobs }, [&] { post_sync_work(m, true); });
+        if (!finish()) return S_INTERNAL;
     }
-    if (timing_) cudaEventRecord(ev_[7], s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return S_INTERNAL;
     info_.launches = launch_counter();
     info_.device_status = (int)hs->st.flags;
-    info_.orient_exact = hs->st.pc.orient_exact;
-    info_.incircle_exact = hs->st.pc.incircle_exact;
+    take_pred_stats(info_, hs->st);
     info_.ntri = m >= 3 ? hs->words[1] : 0;
     if (hs->st.flags & (ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX)) return S_INTERNAL;
     if (timing_)

@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 
+#include "common.cuh"
 #include "mesh_layout.hpp"
 #include "mesh_mirror.hpp"
 
@@ -89,17 +90,42 @@ struct StageTimes
     float h2d = 0, keys_sort = 0, unique = 0, split = 0, build = 0, extract = 0, d2h = 0, total = 0;
 };
 
+// Predicate statistics of one stage (common.cuh PredCounters)
+struct PredStats
+{
+    unsigned long long calls[2] = { 0, 0 }, f32_undecided[2] = { 0, 0 }, exact[2] = { 0, 0 };
+};
+
 struct RunInfo
 {
     size_t                 n = 0, unique_points = 0, ntri = 0;
-    unsigned long long     orient_exact = 0, incircle_exact = 0;
+    unsigned long long     orient_exact = 0, incircle_exact = 0;   // sums over the stages
+    PredStats              stage[kPredStages];
     StageTimes             ms;
     int                    device_status = 0;
     int                    launches = 0;
     int                    window = 0;   // warp merges' candidate window of the last call
+    int                    wide = 0;     // the build ran again with the widest exact tier
 };
 
 struct DeviceWork;
+
+// copies the predicate statistics of a call's device status into its RunInfo
+inline void take_pred_stats(RunInfo& info, const DevStatus& st)
+{
+    info.orient_exact = info.incircle_exact = 0;
+    for (int s = 0; s < kPredStages; ++s)
+    {
+        for (int k = 0; k < 2; ++k)
+        {
+            info.stage[s].calls[k] = st.pc[s].calls[k];
+            info.stage[s].f32_undecided[k] = st.pc[s].f32_undecided[k];
+            info.stage[s].exact[k] = st.pc[s].exact[k];
+        }
+        info.orient_exact += st.pc[s].exact[0];
+        info.incircle_exact += st.pc[s].exact[1];
+    }
+}
 
 // device bytes of a many-set workspace for N points in S sets (batch.cu)
 size_t bcarve_bytes(size_t N, size_t S);
@@ -190,7 +216,7 @@ private:
     Engine() = default;
     int  ensure(size_t n);
     int  pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tri_cap, uint32_t* host_rep);
-    void post_sync_work(size_t m);
+    void post_sync_work(size_t m, bool wide);
     void clear_graphs() noexcept;
     // runs work() on stream(): replayed from the graph cached under key, or
     // captured into one first; launch by launch when graphs are off or fail

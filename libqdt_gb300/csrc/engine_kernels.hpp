@@ -91,8 +91,16 @@ void launch_finalize(const PrepBuffers& b, int m, cudaStream_t s);
 int mesh_build_device(const uint32_t* tris, const double2* pts, size_t n, size_t T, cudaStream_t s,
     MeshMirror& mir, MeshVec<int>& o2l, MeshVec<MeshVertex>& v, MeshVec<MeshHalfEdge>& h);
 
-// builds every level from the deepest to the root
+// builds every level from the deepest to the root, then extracts the
+// triangles: narrow, the kernels without the widest exact tier (every call);
+// wide, with it (a call whose predicates needed it, run again)
+namespace narrow {
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s);
 void launch_extract(const BuildBuffers& b, int m, cudaStream_t s);
+}  // namespace narrow
+namespace wide {
+void launch_build(const BuildBuffers& b, int m, cudaStream_t s);
+void launch_extract(const BuildBuffers& b, int m, cudaStream_t s);
+}  // namespace wide
 
 }  // namespace qdtg

@@ -24,6 +24,15 @@
 // * every record access is bounds-checked and every loop has an iteration
 //   guard; a violation sets a device status bit and ends the thread, and the
 //   host reports QDT_ERR_INTERNAL. No trap, no hang.
+// This file is compiled twice: here with QDTG_WIDE_EXACT 0 (kernels in
+// qdtg::narrow, without the widest exact tier, run on every call), and from
+// k_build_wide.cu with it (qdtg::wide, run again on the rare call whose
+// predicates needed that tier; see predicates.cuh).
+#ifndef QDTG_BUILD_VARIANT
+#define QDTG_WIDE_EXACT 0
+#define QDTG_BUILD_VARIANT narrow
+#endif
+
 #include "builder.cuh"
 #include "common.cuh"
 #include "engine_kernels.hpp"
@@ -31,8 +40,7 @@
 #include "scan.cuh"
 
 namespace qdtg {
-
-
+namespace QDTG_BUILD_VARIANT {
 
 // One depth of the tree: leaves of that depth are built, internal nodes merge
 // their children's results (written by the previous launch). WARP: one node
@@ -50,8 +58,9 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
     if (flags & kFatal) return;
     int lo, hi;
     if (!node_range(m, d, k, lo, hi)) return;
-    Builder B{ R, nrec, st, count ? &st->pc : nullptr, -1, -1, false };
     const int n = hi - lo;
+    Builder   B{ R, nrec, st, pred_stage(st, n <= 3 ? kStageLeaf : (WARP ? kStageWarp : kStageThread), count), -1, -1,
+        false };
     NodeOut   o;
     o.le2 = o.re2 = -1;
     o.pad0 = o.pad1 = 0;
@@ -198,7 +207,7 @@ __global__ void __launch_bounds__(kCellBlockWarps * 32) k_build_cells(Rec* __res
     if (flags & kFatal) return;
     int lo, hi;
     if (!node_range(m, dc, k, lo, hi) || hi - lo > C) return;
-    build_cell(cell_smem + w * cell_smem_bytes(C), V, R, lo, hi, dc, st, count ? &st->pc : nullptr, out + k);
+    build_cell(cell_smem + w * cell_smem_bytes(C), V, R, lo, hi, dc, st, pred_stage(st, kStageThread, count), out + k);
 }
 
 // Depths with at most b.warp_nodes nodes run one node per warp (few merges:
@@ -300,7 +309,7 @@ __global__ void k_tri_mask(const Rec* __restrict__ R, int nrec, uint8_t* __restr
         mask[k] = 0;
         return;
     }
-    Builder B{ const_cast<Rec*>(R), nrec, st, count ? &st->pc : nullptr, -1, -1, false };
+    Builder B{ const_cast<Rec*>(R), nrec, st, pred_stage(st, kStageExtract, count), -1, -1, false };
     uint8_t mk = 0;
     if (R[k].org[0] >= 0)
     {
@@ -354,4 +363,5 @@ void launch_extract(const BuildBuffers& b, int m, cudaStream_t s)
     ++launch_counter();
 }
 
+}  // namespace QDTG_BUILD_VARIANT
 }  // namespace qdtg

@@ -87,6 +87,31 @@ QDT_HD __forceinline__ double sub_rn(double a, double b)
 #endif
 }
 
+// Counters passed to the predicates: a tagged pointer (bit 0: count calls)
+QDT_HD __forceinline__ PredCounters* pc_of(PredCounters* t)
+{
+    return reinterpret_cast<PredCounters*>(reinterpret_cast<uintptr_t>(t) & ~(uintptr_t)1);
+}
+QDT_HD __forceinline__ bool pc_counts(const PredCounters* t) { return (reinterpret_cast<uintptr_t>(t) & 1u) != 0; }
+// one event per calling lane; on the device one atomic per warp
+QDT_HD __forceinline__ void pc_add(unsigned long long* c)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned mask = __activemask();
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(c, (unsigned long long)__popc(mask));
+#else
+    ++*c;
+#endif
+}
+
+// Counting every call takes code at every call site of the merges: only
+// kernels built with QDTG_COUNT_CALLS 1 (the single-set build's wide
+// variant, which the engine runs when a call counts) have it; elsewhere
+// `calls` stays 0 and only the slow paths are counted.
+#ifndef QDTG_COUNT_CALLS
+#define QDTG_COUNT_CALLS 0
+#endif
+
 constexpr double kEps = 1.1102230246251565e-16;
 constexpr double kErrOrient = (3.0 + 16.0 * kEps) * kEps;
 constexpr double kErrIncircle = (10.0 + 96.0 * kEps) * kEps;
@@ -148,18 +173,19 @@ QDT_HD __forceinline__ void big_trim(BigRef& a)
     if (a.n == 0) a.neg = 0;
 }
 
-// a = m << sh (m < 2^53), with sign
-QDT_HD inline void big_set_shifted(BigRef& a, uint64_t m, int sh, int neg)
+// a = m << sh (m < 2^53), with sign, in at most cap limbs (the limbs past
+// cap are zero: the caller sized cap for the value)
+QDT_HD inline void big_set_shifted(BigRef& a, uint64_t m, int sh, int neg, int cap)
 {
     const int limb = sh >> 5, bit = sh & 31;
     for (int i = 0; i < limb; ++i) a.d[i] = 0;
     // m << bit spans at most 53 + 31 = 84 bits: three limbs
     const uint64_t lo = m << bit;
     const uint64_t hi = bit ? (m >> (64 - bit)) : 0;
-    a.d[limb + 0] = (uint32_t)lo;
-    a.d[limb + 1] = (uint32_t)(lo >> 32);
-    a.d[limb + 2] = (uint32_t)hi;
-    a.n = limb + 3;
+    const uint32_t w[3] = { (uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi };
+    int            n = limb;
+    for (int i = 0; i < 3 && limb + i < cap; ++i) a.d[n++] = w[i];
+    a.n = n;
     a.neg = neg;
     big_trim(a);
 }
@@ -269,29 +295,35 @@ QDT_HD inline void big_mul(BigRef& r, const BigRef& a, const BigRef& b)
 
 QDT_HD __forceinline__ int big_sign(const BigRef& a) { return a.n == 0 ? 0 : (a.neg ? -1 : 1); }
 
-// Coordinates of one predicate as integers N_i * 2^E.
+// Coordinates of one predicate as integers N_i * 2^E: E (emin) and the
+// largest bit length of |N_i| (width); each N_i is formed from its double
+// when it is needed (the loops over the coordinates are unrolled, so the
+// doubles stay in registers and no per-coordinate table takes stack space).
 template <int K>
 struct IntCoords
 {
-    Dec d[K];
-    int emin;
-    int width;   // max bit length of |N_i|
+    double v[K];
+    int    emin;
+    int    width;
 };
 
 template <int K>
-QDT_HD inline void int_coords(const double* v, IntCoords<K>& c)
+QDT_HD __forceinline__ void int_coords(IntCoords<K>& c)
 {
     c.emin = 1 << 20;
+#pragma unroll
     for (int i = 0; i < K; ++i)
     {
-        c.d[i] = decompose(v[i]);
-        if (c.d[i].m && c.d[i].e < c.emin) c.emin = c.d[i].e;
+        const Dec d = decompose(c.v[i]);
+        if (d.m && d.e < c.emin) c.emin = d.e;
     }
     c.width = 0;
+#pragma unroll
     for (int i = 0; i < K; ++i)
     {
-        if (!c.d[i].m) continue;
-        const int w = bitlen64(c.d[i].m) + (c.d[i].e - c.emin);
+        const Dec d = decompose(c.v[i]);
+        if (!d.m) continue;
+        const int w = bitlen64(d.m) + (d.e - c.emin);
         if (w > c.width) c.width = w;
     }
 }
@@ -299,58 +331,60 @@ QDT_HD inline void int_coords(const double* v, IntCoords<K>& c)
 template <int K>
 QDT_HD __forceinline__ int64_t int_small(const IntCoords<K>& c, int i)
 {
-    if (!c.d[i].m) return 0;
-    const int64_t x = (int64_t)(c.d[i].m << (c.d[i].e - c.emin));
-    return c.d[i].neg ? -x : x;
+    const Dec d = decompose(c.v[i]);
+    if (!d.m) return 0;
+    const int64_t x = (int64_t)(d.m << (d.e - c.emin));
+    return d.neg ? -x : x;
 }
 
 // The widest coordinate span a predicate can have: from the top bit of the
 // largest double (2^1023 * (2 - 2^-52)) to the lowest bit of the smallest
-// subnormal (2^-1074): 2098 bits, 66 limbs.
-constexpr int kCoordLimbs = 68;               // a coordinate difference
-constexpr int kProdLimbs = 2 * kCoordLimbs + 1;
-constexpr int kDetLimbs = 2 * kProdLimbs + 2;
+// subnormal (2^-1074): 2098 bits, 66 limbs. Limb counts of the two
+// multi-limb tiers: CL limbs hold a coordinate.
+template <int CL>
+struct Limbs
+{
+    static constexpr int coord = CL + 1;          // a difference of two CL-limb coordinates
+    static constexpr int prod = 2 * coord + 1;    // a product of two differences, a sum of two
+    static constexpr int det = 2 * prod + 2;      // a product of two such sums, a sum of three
+};
+constexpr int kMidLimbs = 3;    // spans of up to 95 bits: circles, clustered and snapped points
+constexpr int kWideLimbs = 67;  // any span
+constexpr int kMidWidth = 32 * kMidLimbs - 1;
 
 template <int K>
-QDT_HD inline void big_coord(BigRef& r, const IntCoords<K>& c, int i)
+QDT_HD inline void big_coord(BigRef& r, const IntCoords<K>& c, int i, int cap)
 {
-    if (!c.d[i].m)
+    const Dec d = decompose(c.v[i]);
+    if (!d.m)
     {
         r.n = 0;
         r.neg = 0;
         return;
     }
-    big_set_shifted(r, c.d[i].m, c.d[i].e - c.emin, c.d[i].neg);
+    big_set_shifted(r, d.m, d.e - c.emin, d.neg, cap);
 }
 
-// exact sign of (ax-cx)(by-cy) - (ay-cy)(bx-cx); v = {ax, ay, bx, by, cx, cy}
-static QDT_HD __noinline__ int orient2d_exact(const double* v)
+// sign of (ax-cx)(by-cy) - (ay-cy)(bx-cx) in CL-limb arithmetic
+template <int CL>
+QDT_HD inline int orient2d_limbs(const IntCoords<6>& c)
 {
-    IntCoords<6> c;
-    int_coords<6>(v, c);
-    if (c.width <= 62)
-    {
-        const int64_t ax = int_small(c, 0), ay = int_small(c, 1), bx = int_small(c, 2), by = int_small(c, 3),
-                      cx = int_small(c, 4), cy = int_small(c, 5);
-        const __int128 l = (__int128)(ax - cx) * (__int128)(by - cy);
-        const __int128 r = (__int128)(ay - cy) * (__int128)(bx - cx);
-        return l > r ? 1 : (l < r ? -1 : 0);
-    }
-    uint32_t s0[kCoordLimbs], s1[kCoordLimbs], s2[kCoordLimbs], s3[kCoordLimbs];
-    uint32_t p0[kProdLimbs], p1[kProdLimbs];
+    using L = Limbs<CL>;
+    uint32_t s0[L::coord], s1[L::coord], s2[L::coord], s3[L::coord];
+    uint32_t p0[L::prod], p1[L::prod];
     BigRef   acx{ s0, 0, 0 }, acy{ s1, 0, 0 }, bcx{ s2, 0, 0 }, bcy{ s3, 0, 0 };
     BigRef   t{ p0, 0, 0 };
-    big_coord(acx, c, 0);
-    big_coord(t, c, 4);
+    big_coord(acx, c, 0, CL);
+    big_coord(t, c, 4, CL);
     big_addsub(acx, acx, t, 1);
-    big_coord(acy, c, 1);
-    big_coord(t, c, 5);
+    big_coord(acy, c, 1, CL);
+    big_coord(t, c, 5, CL);
     big_addsub(acy, acy, t, 1);
-    big_coord(bcx, c, 2);
-    big_coord(t, c, 4);
+    big_coord(bcx, c, 2, CL);
+    big_coord(t, c, 4, CL);
     big_addsub(bcx, bcx, t, 1);
-    big_coord(bcy, c, 3);
-    big_coord(t, c, 5);
+    big_coord(bcy, c, 3, CL);
+    big_coord(t, c, 5, CL);
     big_addsub(bcy, bcy, t, 1);
     BigRef l{ p0, 0, 0 }, r{ p1, 0, 0 };
     big_mul(l, acx, bcy);
@@ -359,54 +393,116 @@ static QDT_HD __noinline__ int orient2d_exact(const double* v)
     return big_sign(l);
 }
 
-// exact sign of the in-circle determinant; v = {ax, ay, bx, by, cx, cy, dx, dy}
-static QDT_HD __noinline__ int incircle_exact(const double* v)
+// sign of the in-circle determinant in CL-limb arithmetic
+template <int CL>
+QDT_HD inline int incircle_limbs(const IntCoords<8>& c)
 {
-    IntCoords<8> c;
-    int_coords<8>(v, c);
+    using L = Limbs<CL>;
+    // term_l serves as the scratch of the differences and of the partial
+    // products before it holds each term
+    uint32_t dxs[6][L::coord];
+    uint32_t lift_l[L::prod], cr_l[L::prod];
+    uint32_t term_l[L::det], acc_l[L::det + 2];
+    BigRef   D[6];
+    BigRef   t{ term_l, 0, 0 };
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+    {
+        D[i] = BigRef{ dxs[i], 0, 0 };
+        big_coord(D[i], c, i, CL);
+        big_coord(t, c, 6 + (i & 1), CL);
+        big_addsub(D[i], D[i], t, 1);
+    }
+    // D = {adx, ady, bdx, bdy, cdx, cdy}; term k: lift(k) * cross(k), with
+    // (k, i, j) in {(a,b,c), (b,c,a), (c,a,b)}
+    BigRef acc{ acc_l, 0, 0 };
+    for (int k = 0; k < 3; ++k)
+    {
+        const int i = (k + 1) % 3, j = (k + 2) % 3;
+        BigRef    lift{ lift_l, 0, 0 }, q{ term_l, 0, 0 }, cr{ cr_l, 0, 0 }, term{ term_l, 0, 0 };
+        big_mul(lift, D[2 * k], D[2 * k]);
+        big_mul(q, D[2 * k + 1], D[2 * k + 1]);
+        big_addsub(lift, lift, q, 0);
+        big_mul(cr, D[2 * i], D[2 * j + 1]);
+        big_mul(q, D[2 * j], D[2 * i + 1]);
+        big_addsub(cr, cr, q, 1);
+        big_mul(term, lift, cr);
+        big_addsub(acc, acc, term, 0);
+    }
+    return big_sign(acc);
+}
+
+// Device code compiled with QDTG_WIDE_EXACT 0 (the single-set build's
+// default kernels) has no room for the widest tier: a predicate whose
+// coordinates span more than kMidWidth bits sets `wide` in its counters and
+// answers 0, and the engine runs the call again with the kernels built with
+// QDTG_WIDE_EXACT 1. That keeps the 67-limb arrays, and the local memory the
+// driver reserves for them on every resident thread, out of the kernels that
+// run every call.
+#ifndef QDTG_WIDE_EXACT
+#define QDTG_WIDE_EXACT 1
+#endif
+#if defined(__CUDA_ARCH__) && !QDTG_WIDE_EXACT
+#define QDTG_WIDE_TIER(call)                          \
+    do                                                \
+    {                                                 \
+        if (ctr) atomicOr(&pc_of(ctr)->wide, 1u);     \
+        return 0;                                     \
+    } while (0)
+#else
+#define QDTG_WIDE_TIER(call) return call
+#endif
+
+// exact sign of (ax-cx)(by-cy) - (ay-cy)(bx-cx); out of line, like the
+// filter that calls it, so the merge loops stay small
+static QDT_HD __noinline__ int orient2d_exact_sign(double ax, double ay, double bx, double by, double cx, double cy,
+    PredCounters* ctr)
+{
+    IntCoords<6> c{ { ax, ay, bx, by, cx, cy }, 0, 0 };
+    int_coords<6>(c);
+    if (c.width <= 62)
+    {
+        const int64_t ax_ = int_small(c, 0), ay_ = int_small(c, 1), bx_ = int_small(c, 2), by_ = int_small(c, 3),
+                      cx_ = int_small(c, 4), cy_ = int_small(c, 5);
+        const __int128 l = (__int128)(ax_ - cx_) * (__int128)(by_ - cy_);
+        const __int128 r = (__int128)(ay_ - cy_) * (__int128)(bx_ - cx_);
+        return l > r ? 1 : (l < r ? -1 : 0);
+    }
+    if (c.width <= kMidWidth) return orient2d_limbs<kMidLimbs>(c);
+    QDTG_WIDE_TIER(orient2d_limbs<kWideLimbs>(c));
+}
+
+// exact sign of the in-circle determinant of a, b, c, d
+static QDT_HD __noinline__ int incircle_exact_sign(double ax, double ay, double bx, double by, double cx, double cy,
+    double dx, double dy, PredCounters* ctr)
+{
+    IntCoords<8> c{ { ax, ay, bx, by, cx, cy, dx, dy }, 0, 0 };
+    int_coords<8>(c);
     if (c.width <= 29)
     {
         // |N| < 2^29: differences < 2^30, lifts < 2^61, cross terms < 2^61,
         // terms < 2^122, sum < 2^124
-        const int64_t dx = int_small(c, 6), dy = int_small(c, 7);
-        const int64_t adx = int_small(c, 0) - dx, ady = int_small(c, 1) - dy;
-        const int64_t bdx = int_small(c, 2) - dx, bdy = int_small(c, 3) - dy;
-        const int64_t cdx = int_small(c, 4) - dx, cdy = int_small(c, 5) - dy;
+        const int64_t dx_ = int_small(c, 6), dy_ = int_small(c, 7);
+        const int64_t adx = int_small(c, 0) - dx_, ady = int_small(c, 1) - dy_;
+        const int64_t bdx = int_small(c, 2) - dx_, bdy = int_small(c, 3) - dy_;
+        const int64_t cdx = int_small(c, 4) - dx_, cdy = int_small(c, 5) - dy_;
         const int64_t al = adx * adx + ady * ady, bl = bdx * bdx + bdy * bdy, cl = cdx * cdx + cdy * cdy;
         const int64_t ca = bdx * cdy - cdx * bdy, cb = cdx * ady - adx * cdy, cc = adx * bdy - bdx * ady;
         const __int128 det = (__int128)al * ca + (__int128)bl * cb + (__int128)cl * cc;
         return det > 0 ? 1 : (det < 0 ? -1 : 0);
     }
-    uint32_t dxs[6][kCoordLimbs];
-    BigRef   D[6];
-    uint32_t tl[kCoordLimbs];
-    BigRef   t{ tl, 0, 0 };
-    for (int i = 0; i < 6; ++i)
-    {
-        D[i] = BigRef{ dxs[i], 0, 0 };
-        big_coord(D[i], c, i);
-        big_coord(t, c, 6 + (i & 1));
-        big_addsub(D[i], D[i], t, 1);
-    }
-    // D = {adx, ady, bdx, bdy, cdx, cdy}
-    uint32_t lift_l[kProdLimbs + 1], cr_l[kProdLimbs + 1], q0_l[kProdLimbs], q1_l[kProdLimbs];
-    uint32_t term_l[kDetLimbs], acc_l[kDetLimbs + 2];
-    BigRef   acc{ acc_l, 0, 0 };
-    // term k: lift(k) * cross(k), with (k, i, j) in {(a,b,c), (b,c,a), (c,a,b)}
-    for (int k = 0; k < 3; ++k)
-    {
-        const int i = (k + 1) % 3, j = (k + 2) % 3;
-        BigRef    lift{ lift_l, 0, 0 }, q0{ q0_l, 0, 0 }, q1{ q1_l, 0, 0 }, cr{ cr_l, 0, 0 }, term{ term_l, 0, 0 };
-        big_mul(q0, D[2 * k], D[2 * k]);
-        big_mul(q1, D[2 * k + 1], D[2 * k + 1]);
-        big_addsub(lift, q0, q1, 0);
-        big_mul(q0, D[2 * i], D[2 * j + 1]);
-        big_mul(q1, D[2 * j], D[2 * i + 1]);
-        big_addsub(cr, q0, q1, 1);
-        big_mul(term, lift, cr);
-        big_addsub(acc, acc, term, 0);
-    }
-    return big_sign(acc);
+    if (c.width <= kMidWidth) return incircle_limbs<kMidLimbs>(c);
+    QDTG_WIDE_TIER(incircle_limbs<kWideLimbs>(c));
+}
+
+// the same on arrays v = {ax, ay, bx, by, cx, cy} / {ax, ..., dy}
+QDT_HD inline int orient2d_exact(const double* v, PredCounters* ctr = nullptr)
+{
+    return orient2d_exact_sign(v[0], v[1], v[2], v[3], v[4], v[5], ctr);
+}
+QDT_HD inline int incircle_exact(const double* v, PredCounters* ctr = nullptr)
+{
+    return incircle_exact_sign(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], ctr);
 }
 
 // ---------------------------------------------------------------------------
@@ -532,24 +628,21 @@ QDT_HD __forceinline__ int incircle_f32(double adx_, double ady_, double bdx_, d
 static QDT_HD __noinline__ int orient2d_slow(double ax, double ay, double bx, double by, double cx, double cy,
     PredCounters* ctr)
 {
+    if (pc_counts(ctr)) pc_add(&pc_of(ctr)->f32_undecided[0]);
     const double detleft = mul_rn(sub_rn(ax, cx), sub_rn(by, cy));
     const double detright = mul_rn(sub_rn(ay, cy), sub_rn(bx, cx));
     const double det = sub_rn(detleft, detright);
     const double mag = add_rn(fabs(detleft), fabs(detright));
     const double bound = mul_rn(kErrOrient, mag);
     if ((det > bound || -det > bound) && mag > kFilterFloor) return det > 0 ? 1 : -1;
-#ifdef __CUDA_ARCH__
-    if (ctr) atomicAdd(&ctr->orient_exact, 1ull);
-#else
-    if (ctr) ++ctr->orient_exact;
-#endif
-    const double v[6] = { ax, ay, bx, by, cx, cy };
-    return orient2d_exact(v);
+    if (pc_counts(ctr)) pc_add(&pc_of(ctr)->exact[0]);
+    return orient2d_exact_sign(ax, ay, bx, by, cx, cy, ctr);
 }
 
 static QDT_HD __noinline__ int incircle_slow(double ax, double ay, double bx, double by, double cx, double cy,
     double dx, double dy, PredCounters* ctr)
 {
+    if (pc_counts(ctr)) pc_add(&pc_of(ctr)->f32_undecided[1]);
     const double adx = sub_rn(ax, dx), ady = sub_rn(ay, dy);
     const double bdx = sub_rn(bx, dx), bdy = sub_rn(by, dy);
     const double cdx = sub_rn(cx, dx), cdy = sub_rn(cy, dy);
@@ -567,19 +660,17 @@ static QDT_HD __noinline__ int incircle_slow(double ax, double ay, double bx, do
         mul_rn(add_rn(fabs(adxbdy), fabs(bdxady)), clift));
     const double bound = mul_rn(kErrIncircle, perm);
     if ((det > bound || -det > bound) && perm > kFilterFloor) return det > 0 ? 1 : -1;
-#ifdef __CUDA_ARCH__
-    if (ctr) atomicAdd(&ctr->incircle_exact, 1ull);
-#else
-    if (ctr) ++ctr->incircle_exact;
-#endif
-    const double v[8] = { ax, ay, bx, by, cx, cy, dx, dy };
-    return incircle_exact(v);
+    if (pc_counts(ctr)) pc_add(&pc_of(ctr)->exact[1]);
+    return incircle_exact_sign(ax, ay, bx, by, cx, cy, dx, dy, ctr);
 }
 
 QDT_HD __forceinline__ int orient2d_sign(double ax, double ay, double bx, double by, double cx, double cy,
     PredCounters* ctr = nullptr)
 {
     const int s = orient2d_f32(sub_rn(ax, cx), sub_rn(ay, cy), sub_rn(bx, cx), sub_rn(by, cy));
+#if QDTG_COUNT_CALLS
+    if (pc_counts(ctr)) pc_add(&pc_of(ctr)->calls[0]);
+#endif
     return s ? s : orient2d_slow(ax, ay, bx, by, cx, cy, ctr);
 }
 
@@ -588,6 +679,9 @@ QDT_HD __forceinline__ int incircle_sign(double ax, double ay, double bx, double
 {
     const int s = incircle_f32(sub_rn(ax, dx), sub_rn(ay, dy), sub_rn(bx, dx), sub_rn(by, dy), sub_rn(cx, dx),
         sub_rn(cy, dy));
+#if QDTG_COUNT_CALLS
+    if (pc_counts(ctr)) pc_add(&pc_of(ctr)->calls[1]);
+#endif
     return s ? s : incircle_slow(ax, ay, bx, by, cx, cy, dx, dy, ctr);
 }
 

@@ -210,6 +210,55 @@ def test_side_prefetch_same_result(lib):
             assert _digest(O.canonical(ref_tris).astype(np.int64)) == spec["serial"]["tri_digest"]
 
 
+def test_filter_stats_per_stage(lib):
+    """Counting the predicates (per stage: leaves, thread merges, warp
+    merges, extraction) leaves the result unchanged; every stage is counted;
+    undecided counts nest (exact <= float-undecided <= calls); the totals
+    equal run_info's; uniform points never need the exact in-circle, the
+    lattice with duplicates does."""
+    cases = [("uniform", W.uniform(300000, 61), False), ("lattice", W.lattice_with_duplicates(300, 0.01, 62), True)]
+    for name, p, degenerate in cases:
+        with G.Triangulation(lib) as t:
+            assert t.execute(p) == 0
+            plain = O.canonical(t.triangles_array())
+            t.set_options(count_filter_failures=True)
+            assert t.execute(p) == 0
+            assert np.array_equal(O.canonical(t.triangles_array()), plain), name
+            fs = t.filter_stats()
+            info = t.run_info()
+        tot = {"orient2d": 0, "incircle": 0}
+        for stage in ("leaf", "thread", "warp", "extract"):
+            for pred in ("orient2d", "incircle"):
+                c = fs[stage][pred]
+                assert c["exact"] <= c["f32_undecided"] <= c["calls"], (name, stage, pred, c)
+                tot[pred] += c["exact"]
+            assert fs[stage]["orient2d"]["calls"] > 0, (name, stage)
+        assert fs["extract"]["incircle"]["calls"] == 0 and fs["leaf"]["incircle"]["calls"] == 0
+        assert fs["warp"]["incircle"]["calls"] > 0 and fs["thread"]["incircle"]["calls"] > 0
+        assert tot["orient2d"] == info["orient_exact"] and tot["incircle"] == info["incircle_exact"]
+        if degenerate:
+            assert tot["incircle"] > 0 and tot["orient2d"] > 0
+        else:
+            assert tot["incircle"] == 0
+
+
+def test_wide_exact_rerun(lib):
+    """Coordinates that span more than 95 bits inside one predicate need the
+    widest exact tier, which the default build kernels leave out: such a
+    call runs its build again with the kernels that have it (run_info
+    wide_exact), and its triangles are the oracle's. Ordinary inputs never
+    take the second run."""
+    rng = np.random.default_rng(71)
+    base = rng.integers(0, 40, size=(3000, 2)).astype(np.float64)
+    tiny = base.copy()
+    tiny[::7] += np.ldexp(rng.integers(1, 8, size=(tiny[::7].shape[0], 2)).astype(np.float64), -90)
+    for p, wide in ((tiny, 1), (W.uniform(20000, 72), 0), (W.lattice_with_duplicates(60, 0.02, 73), 0)):
+        with G.Triangulation(lib) as t:
+            assert t.execute(p) == 0
+            assert t.run_info()["wide_exact"] == wide
+            assert np.array_equal(O.canonical(t.triangles_array()), O.canonical(O.triangulate(p).tris))
+
+
 def test_merge_window_same_result(lib):
     """The warp merges' candidate window (1 or 2) is a schedule: the same
     triangulation either way; the automatic choice takes 1 on lattice-like
