@@ -39,10 +39,28 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpoints/s triangulated (0 exact violations), single+batched; p50/p99 latency"
 UNIT = "Mpoints/s"
 
-# DRAM bytes (read + written) of the build launches of one call, measured with
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum over every k_build_level
-# launch of the second of two `--profile-run single` calls, one pass each)
-BUILD_TRAFFIC = {"uniform_2p6m": 2_716_100_000 + 1_085_800_000}
+PROFILES = os.path.join(ROOT, "profiles")
+
+
+def profile_traffic(workload, stage="build"):
+    """DRAM bytes (read + written) of one call's launches of a stage, from the
+    `traffic-record:` line of a committed ncu summary under profiles/ (one
+    capture of the workload; the line names the commit it measured). Returns
+    (bytes or None, source dict)."""
+    import glob
+    import re
+    for path in sorted(glob.glob(os.path.join(PROFILES, "*.md"))):
+        with open(path) as f:
+            for line in f:
+                m = re.match(r"\s*traffic-record:\s*(.*)$", line)
+                if not m:
+                    continue
+                kv = dict(t.split("=", 1) for t in m.group(1).split() if "=" in t)
+                if kv.get("workload") == workload and kv.get("stage") == stage:
+                    total = int(kv["dram_read"]) + int(kv["dram_write"])
+                    return total, {"profile": os.path.relpath(path, ROOT), "commit": kv.get("commit"),
+                                   "date": kv.get("date"), "launches": int(kv.get("launches", 0))}
+    return None, {"reason": "no committed ncu capture of this workload's %s stage" % stage}
 
 WORKLOADS = {
     "uniform_2p6m": ("uniform", 2600000, 2),
@@ -298,6 +316,7 @@ def run_gb300(args):
     }
     top = max(stage_ms, key=lambda k: stage_ms[k])
     achieved = (alg[top] or 1) / (stage_ms[top] / 1e3) / 1e9 if stage_ms[top] > 0 else 0.0
+    traffic, traffic_src = profile_traffic(args.workload, top[3:])
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -312,8 +331,9 @@ def run_gb300(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "stage": top[3:], "achieved": round(achieved, 2), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 5),
-                     "traffic": BUILD_TRAFFIC.get(args.workload) if top == "ms_build" else None,
-                     "traffic_per": "one call's build launches (all depths), ncu dram bytes read + written",
+                     "traffic": traffic,
+                     "traffic_per": "one call's %s launches, ncu dram bytes read + written" % top[3:],
+                     "traffic_source": traffic_src,
                      "algorithmic_bytes": alg[top]},
         "clocks": ck,
     }

@@ -36,6 +36,9 @@ typedef struct qdtg_run_info
     int                merge_window;    /* candidate window of the warp merges (1 or 2; 0 = none ran) */
     int                wide_exact;      /* 1: a predicate needed the widest exact tier and the build ran
                                            again with the kernels that have it */
+    int                split_depth;     /* deepest depth whose merges ran with two walkers (-1: none) */
+    int                split_rerun;     /* 1: a two-walker merge could not finish and the build ran
+                                           again with one walker per merge */
 } qdtg_run_info;
 
 /* Options of a context: count_filter_failures != 0 counts the predicate calls
@@ -78,6 +81,17 @@ QDT_API int qdtg_set_split_tail(qdt_t* ptr, int on);
    record numbers it selected and never writes a record, so the result is
    the same either way. Returns 1, or 0 for a NULL context or no usable GPU. */
 QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
+
+/* The merges at the top of the build -- depths 0..max_depth (at most 9)
+   whose nodes hold at least min_points points (at least 4,096) -- run with
+   two walkers each: the reference's rising merge from the lower common
+   tangent and its mirror image from the upper one, which meet at a point of
+   the seam. A merge whose falling walker meets cocircular or collinear
+   points is finished by the rising one, so the triangulation is the same
+   as with one walker per merge (max_depth -1). Defaults 7 and 8,192.
+   Returns 1, or 0 for a NULL context, values out of range or no usable
+   GPU. No counterpart in the reference, whose merges are sequential. */
+QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
 
 /* Caps the device bytes of the context's workspace (0: no cap, the
    default). A batch call whose workspace would exceed the cap returns

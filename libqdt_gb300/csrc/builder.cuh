@@ -7,6 +7,13 @@
 #include "common.cuh"
 #include "predicates.cuh"
 
+#ifndef QDTG_SPLIT_DEBUG
+#define QDTG_SPLIT_DEBUG 0
+#endif
+#if QDTG_SPLIT_DEBUG
+#include <cstdio>
+#endif
+
 // Launch bounds of the level kernels: 128 threads. (A minimum of resident
 // blocks, which would cap the registers, measured no faster: the
 // thread-per-node levels are chains of dependent loads and predicates that
@@ -744,6 +751,10 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
         lstart = B.onext(sym(basel));
         rstart = B.oprev(basel);
     }
+#if QDTG_SPLIT_DEBUG
+    long long dbg_t0 = clock64(), dbg_win = 0, dbg_pred = 0, dbg_conn = 0, dbg_c = 0;
+    int       dbg_steps = 0, dbg_passes = 0;
+#endif
     int it = 0;
     while (!bad)
     {
@@ -763,6 +774,10 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
                 bad = true;
                 break;
             }
+#if QDTG_SPLIT_DEBUG
+            ++dbg_passes;
+            dbg_c = clock64();
+#endif
             // --- the window: kWin + 1 records along this side's ring
             Ent cur = load_ent(R, left ? lstart : rstart, nrec, left);
             Ent mine = cur, succ = cur;
@@ -774,6 +789,14 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
                 if (i == jj + 1) succ = nx;
                 cur = nx;
             }
+#if QDTG_SPLIT_DEBUG
+            {
+                const int sink = __shfl_sync(FULL, cur.e ^ mine.e ^ succ.e, 0);
+                const long long c1 = clock64() + (sink & 0);
+                dbg_win += c1 - dbg_c;
+                dbg_c = c1;
+            }
+#endif
             // --- one wave of predicates
             const int     src_a = combo ? ca : 0, src_b = combo ? 16 + rb : 16;
             const int     ad = __shfl_sync(FULL, mine.d, src_a), bdst = __shfl_sync(FULL, mine.d, src_b);
@@ -794,6 +817,13 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
             const unsigned zl = ~il & 0xFu, zr = ~ir & 0xFu;
             const int      dl = (cont_l || (vl & 1u)) ? (zl ? __ffs(zl) - 1 : kWin) : 0;
             const int      dr = (cont_r || (vr & 1u)) ? (zr ? __ffs(zr) - 1 : kWin) : 0;
+#if QDTG_SPLIT_DEBUG
+            {
+                const long long c1 = clock64();
+                dbg_pred += c1 - dbg_c;
+                dbg_c = c1;
+            }
+#endif
             // the candidate each scan stops at: slot dl (slot kWin is the
             // successor of slot kWin - 1)
             const int  srcL = min(dl, kWin - 1), srcR = 16 + min(dr, kWin - 1);
@@ -860,6 +890,10 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
             break;
         }
         if (bad || (!lv && !rv)) break;
+#if QDTG_SPLIT_DEBUG
+        const long long dbg_cc = clock64();
+        ++dbg_steps;
+#endif
         // --- the new base edge (builder.hxx:279-282), from window values only
         const bool take_r = !lv || (rv && choice);
         const int  k = fhead;
@@ -905,7 +939,15 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
         rstart = x0;   // oprev(e)
         if (fhead >= 0) flink = recof(R, 2 * fhead, nrec).link;
         __syncwarp();
+#if QDTG_SPLIT_DEBUG
+        dbg_conn += clock64() - dbg_cc;
+#endif
     }
+#if QDTG_SPLIT_DEBUG
+    if (lane == 0 && B.nrec > 0 && first_out && dbg_steps > 300)
+        printf("warp merge steps=%d passes=%d cyc=%lld win=%lld pred=%lld conn=%lld\n", dbg_steps, dbg_passes,
+            clock64() - dbg_t0, dbg_win, dbg_pred, dbg_conn);
+#endif
     if (lane == 0)
     {
         B.fhead = fhead;
@@ -916,7 +958,7 @@ static __device__ void warp_merge(Builder& B, int ldo, int ldi, int rdi, int rdo
     out_r = __shfl_sync(FULL, rdo, 0);
 }
 
-constexpr unsigned kFatal = ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX;
+constexpr unsigned kFatal = ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX | ST_SPLIT;
 
 // ---------------------------------------------------------------------------
 // Cells: the bottom of the tree in shared memory

@@ -570,6 +570,8 @@ QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
     info->kernel_launches = r.launches;
     info->merge_window = r.window;
     info->wide_exact = r.wide;
+    info->split_depth = r.split_depth;
+    info->split_rerun = r.split_rerun;
     return 1;
 }
 
@@ -597,6 +599,15 @@ QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on)
     if (!c) return 0;
     if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
     c->engine->set_side_prefetch(on != 0);
+    return 1;
+}
+
+QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points)
+{
+    Context* c = ctx(ptr);
+    if (!c || max_depth < -1 || max_depth > qdtg::kSplitMaxDepth || min_points < qdtg::kSplitFloor) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_split(max_depth, min_points);
     return 1;
 }
 

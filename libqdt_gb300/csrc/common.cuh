@@ -51,6 +51,7 @@ enum StatusBits : unsigned
     ST_POOL_EMPTY = 2u,      // a node's free list ran dry (cannot happen with a sound 3n bound)
     ST_GUARD = 4u,           // a loop exceeded its iteration guard (internal error)
     ST_BAD_INDEX = 8u,       // an index left its node's range (internal error)
+    ST_SPLIT = 16u,          // a split merge could not finish: the call runs again without them
 };
 
 // Predicate statistics of one stage of a call ([0] orient2d, [1] in-circle):
@@ -93,6 +94,30 @@ __host__ __device__ inline PredCounters* pred_stage(DevStatus* st, int stage, in
 // Depths whose seams (cut coordinates) are recorded during the split, and whose
 // seam records are prefetched into L2 before they merge.
 constexpr int kSeamDepth = 10;
+
+// Split merges (seam_split.cuh): at most these depths (their children's cuts
+// are recorded), nodes of at least kSplitFloor points.
+constexpr int kSplitMaxDepth = 9;
+constexpr int kSplitFloor = 4096;
+constexpr int kSplitDefaultDepth = 7;
+constexpr int kSplitDefaultPoints = 8192;
+// bins of the records near a split merge's seam, along it (where its two
+// walkers meet)
+constexpr int kSeamBins = 64;
+
+// The split merges of one call: depths 0..depth, each walker of a node of
+// depth d with per[d] spare records (ids spare0 + base[d] + 2 per[d] k + w
+// per[d], w = 0 rising, 1 falling) and as many deletion-list entries (lists
+// + the same offset); spare records in all.
+struct SplitPlan
+{
+    int       depth = -1;
+    int       spare0 = 0;
+    int       spare = 0;
+    int       per[kSplitMaxDepth + 1] = {};
+    long long base[kSplitMaxDepth + 1] = {};
+    int*      lists = nullptr;
+};
 
 // Largest cell (points) built in shared memory: 6 * kCellMax half-edge ids
 // fit in the 16-bit ids of the cell's records.

@@ -1,5 +1,6 @@
 // Host orchestration of the GB300 batch triangulation engine: device
 // workspace, the stage sequence on the context's stream, and the transfers.
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <thread>
@@ -54,6 +55,14 @@ struct Carver
     }
 };
 
+// spare records (and deletion-list entries) of the split merges of N points
+// at every depth they may run at
+size_t split_capacity(size_t N)
+{
+    SplitPlan plan;
+    return (size_t)split_plan((int)std::min<size_t>(N, (size_t)INT32_MAX / 4), kSplitMaxDepth, kSplitFloor, plan);
+}
+
 size_t carve(DeviceWork& w, char* base, size_t N)
 {
     Carver c{ base };
@@ -92,11 +101,14 @@ size_t carve(DeviceWork& w, char* base, size_t N)
     p.status = c.take<DevStatus>(1);
     w.words = c.take<uint32_t>(8);
     p.status_u32 = w.words;
-    b.recs = c.take<Rec>(3 * N);
+    const size_t spare = split_capacity(N);
+    b.recs = c.take<Rec>(3 * N + spare);
     b.V = p.V;
     b.vid = p.vid;
-    b.tri_mask = c.take<uint8_t>(3 * N);
-    b.tri_off = c.take<uint32_t>(3 * N);
+    b.tri_mask = c.take<uint8_t>(3 * N + spare);
+    b.tri_off = c.take<uint32_t>(3 * N + spare);
+    b.split.lists = c.take<int>(spare);
+    b.seam_hist = c.take<unsigned long long>(((size_t)2 << kSplitMaxDepth) * kSeamBins);
     b.scratch = p.scratch;
     b.tris = c.take<uint32_t>(6 * N + 3);
     b.tri_count = w.words + 1;
@@ -105,6 +117,31 @@ size_t carve(DeviceWork& w, char* base, size_t N)
 }
 
 }  // namespace
+
+int split_plan(int m, int max_depth, int min_points, SplitPlan& plan)
+{
+    plan.depth = -1;
+    plan.spare0 = 3 * m;
+    plan.spare = 0;
+    min_points = std::max(min_points, kSplitFloor);
+    long long base = 0;
+    for (int d = 0; d <= std::min(max_depth, kSplitMaxDepth); ++d)
+    {
+        // the largest node of depth d
+        const long long n = ((long long)m + (1ll << d) - 1) >> d;
+        if (n < min_points) break;
+        // each walker: about half the seam's cross edges (3 per sqrt(n)
+        // leaves room for clustered points; a walker that runs out stops or
+        // frees its deleted edges first)
+        const int per = (int)(3.0 * std::sqrt((double)n)) + 128;
+        plan.per[d] = per;
+        plan.base[d] = base;
+        base += 2ll * per * (1ll << d);
+        plan.depth = d;
+    }
+    plan.spare = (int)base;
+    return plan.spare;
+}
 
 Engine* Engine::create(int* cuda_error)
 {
@@ -299,7 +336,9 @@ void Engine::post_sync_work(size_t m, bool wide)
     cudaStream_t  s = stream_;
     PrepBuffers&  p = w_->prep;
     BuildBuffers& b = w_->build;
-    if (wide) cudaMemsetAsync(&p.status->flags, 0, sizeof(unsigned), s);   // the narrow pass's bits
+    // the bits of the stages before (read by the host already) or of a first
+    // pass of the same call
+    cudaMemsetAsync(&p.status->flags, 0, sizeof(unsigned), s);
     // the predicates' counters (the narrow pass's, for a wide one)
     cudaMemsetAsync(&p.status->pc[0], 0, sizeof(p.status->pc), s);
     launch_frames(p, m, s);
@@ -435,19 +474,32 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     b.window = window_ ? window_ : (16ull * hs->words[2] > (unsigned long long)kTieWindow * m ? 1 : 2);
     info_.window = b.window;
     info_.wide = 0;
+    info_.split_rerun = 0;
+    // the top merges with two walkers, except on lattice-like input (the
+    // window-1 test above): there nearly every in-circle test is a tie, the
+    // falling walker stops at its first, and the rising one walks alone
+    {
+        int* lists = b.split.lists;
+        if (split_depth_ >= 0 && b.window != 1) split_plan((int)m, split_depth_, split_min_, b.split);
+        else b.split.depth = -1;
+        b.split.lists = lists;
+    }
+    info_.split_depth = b.split.depth;
+    // the stages after the count depend only on m and the knobs: one CUDA
+    // graph per such key (about 250 launches at 2.6 M points)
+    auto knobs_of = [&](bool wide_kernels) {
+        return ((uint64_t)(b.cell_points & 0x7FF) << 4) | ((uint64_t)b.window << 15) |
+               ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
+               ((uint64_t)(p.split_tail ? 1 : 0) << 19) | ((uint64_t)(uint32_t)b.warp_nodes << 20) |
+               ((uint64_t)(b.side ? 1 : 0) << 52) | ((uint64_t)((b.split.depth + 1) & 0xF) << 53) |
+               (wide_kernels ? (1ull << 57) : 0ull);
+    };
     if (m >= 3)
     {
-        // the stages after the count depend only on m and the knobs: one
-        // CUDA graph per such key (about 250 launches at 2.6 M points)
-        const uint64_t knobs = ((uint64_t)(b.cell_points & 0x7FF) << 4) | ((uint64_t)b.window << 15) |
-                               ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
-                               ((uint64_t)(p.split_tail ? 1 : 0) << 19) |
-                               ((uint64_t)(uint32_t)b.warp_nodes << 20) | ((uint64_t)(b.side ? 1 : 0) << 52);
         // a counting call runs the kernels that count every predicate call
         // (the wide ones) from the start
         const bool counting = b.count_filter != 0;
-        run_graph({ (uint64_t)m, knobs | (counting ? (1ull << 57) : 0ull) },
-            [&] { post_sync_work(m, counting); });
+        run_graph({ (uint64_t)m, knobs_of(counting) }, [&] { post_sync_work(m, counting); });
         info_.wide = counting ? 1 : 0;
     }
     else
@@ -474,6 +526,17 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         return cudaStreamSynchronize(s) == cudaSuccess;
     };
     if (!finish()) return S_INTERNAL;
+    if (m >= 3 && (hs->st.flags & ST_SPLIT))
+    {
+        // a split merge could not finish: the stages after the count once
+        // more, every merge with one walker
+        info_.split_rerun = 1;
+        b.split.depth = -1;
+        info_.split_depth = -1;
+        const bool w = info_.wide != 0;
+        run_graph({ (uint64_t)m, knobs_of(w) }, [&] { post_sync_work(m, w); });
+        if (!finish()) return S_INTERNAL;
+    }
     bool wide = false;
     for (int sg = 0; sg < kPredStages; ++sg) wide = wide || hs->st.pc[sg].wide;
     if (m >= 3 && wide && !info_.wide)
@@ -482,19 +545,23 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         // kernels leave out: the stages after the count once more with the
         // kernels that have it
         info_.wide = 1;
-        const uint64_t knobs = ((uint64_t)(b.cell_points & 0x7FF) << 4) | ((uint64_t)b.window << 15) |
-                               ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
-                               ((uint64_t)(p.split_tail ? 1 : 0) << 19) |
-                               ((uint64_t)(uint32_t)b.warp_nodes << 20) | ((uint64_t)(b.side ? 1 : 0) << 52) |
-                               (1ull << 57);
-        run_graph({ (uint64_t)m, knobs }, [&] { post_sync_work(m, true); });
+        run_graph({ (uint64_t)m, knobs_of(true) }, [&] { post_sync_work(m, true); });
+        if (!finish()) return S_INTERNAL;
+    }
+    if (m >= 3 && (hs->st.flags & ST_SPLIT) && b.split.depth >= 0)
+    {
+        // (a wide pass whose split merge failed)
+        info_.split_rerun = 1;
+        b.split.depth = -1;
+        info_.split_depth = -1;
+        run_graph({ (uint64_t)m, knobs_of(true) }, [&] { post_sync_work(m, true); });
         if (!finish()) return S_INTERNAL;
     }
     info_.launches = launch_counter();
     info_.device_status = (int)hs->st.flags;
     take_pred_stats(info_, hs->st);
     info_.ntri = m >= 3 ? hs->words[1] : 0;
-    if (hs->st.flags & (ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX)) return S_INTERNAL;
+    if (hs->st.flags & (ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX | ST_SPLIT)) return S_INTERNAL;
     if (timing_)
     {
         auto el = [&](int a, int z) {

@@ -106,6 +106,8 @@ struct RunInfo
     int                    launches = 0;
     int                    window = 0;   // warp merges' candidate window of the last call
     int                    wide = 0;     // the build ran again with the widest exact tier
+    int                    split_depth = -1;   // deepest depth merged by two walkers (-1: none)
+    int                    split_rerun = 0;    // a split merge failed and the build ran again without them
 };
 
 struct DeviceWork;
@@ -210,6 +212,13 @@ public:
     // the build's seam prefetch on a second stream beside the merges, when
     // no other engine is running a call (default on)
     void            set_side_prefetch(bool on) { side_prefetch_ = on; }
+    // merges of depth at most max_depth whose nodes hold at least min_points
+    // points run with two walkers (seam_split.cuh); max_depth -1: none
+    void            set_split(int max_depth, int min_points)
+    {
+        split_depth_ = max_depth;
+        split_min_ = min_points;
+    }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
@@ -247,6 +256,8 @@ private:
     bool            use_graphs_ = true;
     bool            split_tail_ = true;
     bool            side_prefetch_ = true;
+    int             split_depth_ = kSplitDefaultDepth;
+    int             split_min_ = kSplitDefaultPoints;
     size_t          limit_ = 0;   // workspace bytes cap (0: none)
     bool            capturing_ = false;   // run_graph is recording stream_
     std::map<std::pair<uint64_t, uint64_t>, GraphEntry> graphs_;   // for the current workspace

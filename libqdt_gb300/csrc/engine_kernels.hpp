@@ -44,7 +44,7 @@ struct PrepBuffers
 
 struct BuildBuffers
 {
-    Rec*           recs = nullptr;      // 3 m records
+    Rec*           recs = nullptr;      // 3 m records, then the split merges' spare ones
     const double2* V = nullptr;
     const uint32_t* vid = nullptr;
     NodeOut*       node[2] = { nullptr, nullptr };   // ping-pong per level, 2^D entries
@@ -64,7 +64,14 @@ struct BuildBuffers
     // merges of this one (none: the prefetch runs in line)
     cudaStream_t   side = nullptr;
     cudaEvent_t    fork = nullptr, join = nullptr;
+    SplitPlan      split;               // the top merges with two walkers (depth -1: none)
+    unsigned long long* seam_hist = nullptr; // kSeamBins per node of the split depths (2^(kSplitMaxDepth+1) nodes)
 };
+
+// The split merges of m points: depths 0.. at most max_depth whose nodes
+// hold at least min_points (>= kSplitFloor); plan.spare0 = 3 m, lists left
+// to the caller. Returns the spare records (also plan.spare).
+int split_plan(int m, int max_depth, int min_points, SplitPlan& plan);
 
 // Distinct points sharing x with their predecessor in (x, y) order above
 // this fraction (in 1/16) make the warp merges use a window of one

@@ -38,9 +38,46 @@
 #include "engine_kernels.hpp"
 #include "predicates.cuh"
 #include "scan.cuh"
+#include "seam_split.cuh"
 
 namespace qdtg {
 namespace QDTG_BUILD_VARIANT {
+
+__device__ __forceinline__ bool free_tail_ok(int t, int lo, int hi, int m, int nrec)
+{
+    return (t >= 3 * lo && t < 3 * hi) || (t >= 3 * m && t < nrec);
+}
+
+__device__ __forceinline__ double box_value(unsigned long long k)
+{
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
+// The range of node (d, k) along its seam (y for even d, x for odd d): the
+// bounding box, narrowed by the cuts of its ancestors on that coordinate.
+__device__ inline double2 seam_range(const double* __restrict__ seam, const unsigned long long* __restrict__ box,
+    int d, long long k)
+{
+    double lo = (d & 1) ? box_value(box[0]) : box_value(box[1]);
+    double hi = (d & 1) ? box_value(box[2]) : box_value(box[3]);
+    for (int l = 0; l < d; ++l)
+    {
+        if (((l ^ d) & 1) == 0) continue;   // an ancestor cut on the other coordinate
+        const long long kl = k >> (d - l);
+        const double    c = seam[(1ll << l) + kl];
+        if ((k >> (d - 1 - l)) & 1) lo = fmax(lo, c);
+        else hi = fmin(hi, c);
+    }
+    return make_double2(lo, hi);
+}
+
+__device__ inline int seam_bin(double v, double2 range)
+{
+    const double w = range.y - range.x;
+    if (!(w > 0.0)) return 0;
+    const double t = (v - range.x) / w * kSeamBins;
+    return t <= 0.0 ? 0 : (t >= kSeamBins - 1 ? kSeamBins - 1 : (int)t);
+}
 
 // One depth of the tree: leaves of that depth are built, internal nodes merge
 // their children's results (written by the previous launch). WARP: one node
@@ -73,9 +110,10 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
     else
     {
         const NodeOut L = child[2 * k], Rn = child[2 * k + 1];
-        // the children's free lists lie inside their record ranges
-        if ((L.fhead >= 0 && (L.ftail < 3 * lo || L.ftail >= 3 * hi)) ||
-            (Rn.fhead >= 0 && (Rn.ftail < 3 * lo || Rn.ftail >= 3 * hi)))
+        // the children's free lists lie inside their record ranges (or in
+        // the spare records of split merges, after the pool's 3 m)
+        if ((L.fhead >= 0 && !free_tail_ok(L.ftail, lo, hi, m, nrec)) ||
+            (Rn.fhead >= 0 && !free_tail_ok(Rn.ftail, lo, hi, m, nrec)))
         {
             if (lane == 0) B.fail(ST_BAD_INDEX);
             return;
@@ -128,6 +166,155 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
     out[k] = o;
 }
 
+// The merges of one upper depth with two walkers each (seam_split.cuh): one
+// block of three warps per node, the rising walker, the falling one and the
+// ring inserter. The block's threads then remove the deleted edges
+// together, and its first thread finds the node's extremes.
+template <int WIN>
+__global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, const NodeOut* __restrict__ child,
+    NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count, SplitPlan plan, const double* __restrict__ seam,
+    const unsigned long long* __restrict__ hist, const unsigned long long* __restrict__ box)
+{
+    __shared__ SeamShared S;
+    __shared__ int        go;
+    const long long       k = blockIdx.x;
+    const int             warp = threadIdx.x >> 5;
+    int                   lo = 0, hi = 0;
+    if (threadIdx.x == 0)
+    {
+        go = !(*(volatile unsigned*)&st->flags & kFatal) && k < (1ll << d) && node_range(m, d, k, lo, hi) &&
+             hi - lo >= 4;
+        S.tail[0] = S.tail[1] = 0;
+        S.head[0] = S.head[1] = 0;
+        S.state[0] = S.state[1] = 0;
+        S.last_o = S.last_d = S.last_e = -1;
+        S.first_dn = -1;
+        S.ndel[0] = S.ndel[1] = 0;
+        S.base0 = S.ldo = S.rdo = S.top = -1;
+        S.fhead = S.ftail = -1;
+        S.fail = 0;
+    }
+    __syncthreads();
+    if (!go) return;
+    node_range(m, d, k, lo, hi);
+    const int     n = hi - lo;
+    const NodeOut L = child[2 * k], Rn = child[2 * k + 1];
+    const int     g = (d - 1) & 1;   // the parent's frame
+    if (threadIdx.x == 0)
+    {
+        bool ok = !((L.fhead >= 0 && !free_tail_ok(L.ftail, lo, hi, m, nrec)) ||
+                    (Rn.fhead >= 0 && !free_tail_ok(Rn.ftail, lo, hi, m, nrec)));
+        if (ok)
+        {
+            // the children's free lists, concatenated
+            if (L.fhead >= 0)
+            {
+                S.fhead = L.fhead;
+                if (Rn.fhead >= 0)
+                {
+                    R[L.ftail].link = Rn.fhead;
+                    S.ftail = Rn.ftail;
+                }
+                else
+                    S.ftail = L.ftail;
+            }
+            else
+            {
+                S.fhead = Rn.fhead;
+                S.ftail = Rn.ftail;
+            }
+            if (d > 0) extremes_before_merge(R, nrec, st, &child[2 * k], &child[2 * k + 1], &out[k], g);
+        }
+        else
+        {
+            atomicOr(&st->flags, ST_BAD_INDEX);
+            S.fail = 1;
+        }
+    }
+    __syncthreads();
+    if (S.fail) return;
+    // the meeting point: on the node's cut (x for even d), and along the seam
+    // where half of the records near the seam lie (the histogram of the
+    // seam prefetch), else the mean of the children's cuts
+    const double cut = seam[(1ll << d) + k];
+    double       along = 0.5 * (seam[(1ll << (d + 1)) + 2 * k] + seam[(1ll << (d + 1)) + 2 * k + 1]);
+    if (hist)
+    {
+        const unsigned long long* h = hist + ((1ll << d) + k) * kSeamBins;
+        unsigned long long        total = 0;
+        for (int b = 0; b < kSeamBins; ++b) total += h[b];
+        if (total > 0)
+        {
+            unsigned long long acc = 0;
+            int                b = 0;
+            while (b < kSeamBins - 1 && 2 * (acc + h[b]) < total) acc += h[b++];
+            const double2 rg = seam_range(seam, box, d, k);
+            along = rg.x + (b + 0.5) * ((rg.y - rg.x) / kSeamBins);
+        }
+    }
+    SeamArgs     A;
+    A.R = R;
+    A.nrec = nrec;
+    A.tag = 4u * (unsigned)((1ll << d) + k);
+    A.q = (d & 1) ? make_double2(along, cut) : make_double2(cut, along);
+    const long long off = plan.base[d] + 2ll * plan.per[d] * k;
+    A.a0 = plan.spare0 + (int)(off + (long long)warp * plan.per[d]);
+    A.a1 = A.a0 + plan.per[d];
+    A.list[0] = plan.lists + off;
+    A.list[1] = plan.lists + off + plan.per[d];
+    A.cap = plan.per[d];
+    A.lim = 8 * n + 64;
+    A.frame = d & 1;
+    A.st = st;
+    Builder B{ R, nrec, st, pred_stage(st, kStageWarp, count), S.fhead, S.ftail, false };
+    if (warp == 0) seam_walk<false, WIN>(B, S, A, L.le, L.re, Rn.le, Rn.re);
+    else if (warp == 1) seam_walk<true, WIN>(B, S, A, L.le, L.re, Rn.le, Rn.re);
+    else if ((threadIdx.x & 31) == 0)
+    {
+        bool bad = false;
+        seam_inserter(S, R, nrec, A.tag, bad);
+        if (bad)
+        {
+            atomicOr(&st->flags, ST_SPLIT);
+            S.fail = 1;
+        }
+    }
+    __syncthreads();
+    if (S.fail) return;
+    {
+        bool bad = false;
+        int  fh = S.fhead, ft = S.ftail;
+        seam_apply(R, nrec, A.list[0], S.ndel[0], A.list[1], S.ndel[1], fh, ft, threadIdx.x, (int)blockDim.x,
+            [] { __syncthreads(); }, bad);
+        if (bad) atomicOr(&st->flags, ST_SPLIT);
+        if (threadIdx.x == 0)
+        {
+            S.fhead = fh;
+            S.ftail = ft;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0 || (*(volatile unsigned*)&st->flags & kFatal)) return;
+    NodeOut o;
+    o.pad0 = o.pad1 = 0;
+    int rl = S.ldo, rr = S.rdo;
+    o.le2 = rl;
+    o.re2 = rr;
+    if (d > 0)
+    {
+        *lower_tangent_slot(&out[k]) = S.base0;
+        const int top = S.first_dn >= 0 ? S.first_dn : S.top;
+        const int2 x = extremes_after_merge(R, nrec, st, top, &out[k], &child[2 * k], &child[2 * k + 1], g, n + 8);
+        rl = x.x;
+        rr = x.y;
+    }
+    o.le = rl;
+    o.re = rr;
+    o.fhead = S.fhead;
+    o.ftail = S.fhead >= 0 ? S.ftail : -1;
+    out[k] = o;
+}
+
 // Before an upper depth merges, the records near its seams are fetched into
 // L2 with the evict-last policy: the merges are chains of dependent loads,
 // and their records were last touched by far deeper levels, so without this
@@ -152,8 +339,15 @@ __global__ void k_seam_band(const unsigned long long* __restrict__ box, int m, d
     seam[0] = (m > 0 && a > 0.0 && isfinite(a)) ? kSeamBand * sqrt(a / m) : 0.0;
 }
 
+// hist (split depths, else nullptr): per node, the records within three of
+// their own lengths of the node's cut, counted in kSeamBins bins along the
+// seam. A merge makes about one step per point spacing along its seam, and
+// a band as wide as the local spacing holds about as many records per unit
+// of seam, in dense and sparse parts alike: the counts follow the steps, and
+// the split merge meets at their median.
 __global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int d, const double* __restrict__ seam,
-    uint32_t* __restrict__ list, uint32_t* __restrict__ count, uint32_t cap)
+    uint32_t* __restrict__ list, uint32_t* __restrict__ count, uint32_t cap, unsigned long long* __restrict__ hist,
+    const unsigned long long* __restrict__ box)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
@@ -180,6 +374,11 @@ __global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int
     {
         const uint32_t i = atomicAdd(count, 1u);
         if (i < cap) list[i] = (uint32_t)r;
+        if (hist && dist <= 3.0 * len)
+        {
+            const int bin = seam_bin((d & 1) ? p0.x : p0.y, seam_range(seam, box, d, k));
+            atomicAdd(&hist[((1ll << d) + k) * kSeamBins + bin], 1ull);
+        }
     }
 }
 
@@ -216,7 +415,11 @@ __global__ void __launch_bounds__(kCellBlockWarps * 32) k_build_cells(Rec* __res
 void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
 {
     const int nrec = 3 * m;
-    int       D = split_levels(m);
+    // records in use: the pool, then the split merges' spare records, dead
+    // until a walker takes one
+    const int nall = b.split.depth >= 0 ? nrec + b.split.spare : nrec;
+    if (nall > nrec) cudaMemsetAsync(b.recs + nrec, 0xFF, (size_t)(nall - nrec) * sizeof(Rec), s);
+    int D = split_levels(m);
     const int C = b.cell_points;
     if (C >= 4 && C <= kCellMax)
     {
@@ -243,8 +446,12 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         uint32_t* const list = b.tri_off;
         uint32_t* const count = b.tri_count;
         cudaMemsetAsync(count, 0, sizeof(uint32_t), ps);
+        unsigned long long* const hist = pd <= b.split.depth ? b.seam_hist : nullptr;
+        if (hist)
+            cudaMemsetAsync(hist + ((size_t)1 << pd) * kSeamBins, 0,
+                ((size_t)1 << pd) * kSeamBins * sizeof(unsigned long long), ps);
         k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, ps>>>(b.recs, nrec, m, pd, b.seam, list, count,
-            (uint32_t)nrec);
+            (uint32_t)nrec, hist, b.box);
         k_prefetch_list<<<152 * 8, 256, 0, ps>>>(b.recs, list, count, (uint32_t)nrec);
         launch_counter() += 2;
     };
@@ -262,7 +469,9 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
             else prefetch_depth(d, s);
             pending = false;
         }
-        if (overlap && d >= 1 && d - 1 <= kSeamDepth)
+        // (a split depth's prefetch also sums the seam histogram that places
+        // its meeting points: it runs in line, when no merge edits records)
+        if (overlap && d >= 1 && d - 1 <= kSeamDepth && d - 1 > b.split.depth)
         {
             cudaEventRecord(b.fork, s);
             cudaStreamWaitEvent(b.side, b.fork, 0);
@@ -274,20 +483,31 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         // at those whose nodes hold at least kWarpMinPoints points (the 4 M
         // Gaussian mixture: depth 14, 244 points a node, 72.7 -> 70.2 ms;
         // at 160 points a node, 2.6 M uniform, either form takes the same)
-        if ((1ll << d) <= b.warp_nodes || (m >> d) >= kWarpMinPoints)
+        if (d <= b.split.depth)
+        {
+            // two walkers per merge, one block per node
+            const unsigned long long* hist = prefetch && b.seam_hist ? b.seam_hist : nullptr;
+            if (b.window == 1)
+                k_build_split<1><<<(unsigned)nodes, 96, 0, s>>>(b.recs, nall, b.node[(d + 1) & 1], b.node[d & 1], m,
+                    d, b.status, b.count_filter, b.split, b.seam, hist, b.box);
+            else
+                k_build_split<kWinDefault><<<(unsigned)nodes, 96, 0, s>>>(b.recs, nall, b.node[(d + 1) & 1],
+                    b.node[d & 1], m, d, b.status, b.count_filter, b.split, b.seam, hist, b.box);
+        }
+        else if ((1ll << d) <= b.warp_nodes || (m >> d) >= kWarpMinPoints)
         {
             const unsigned g = (unsigned)((nodes * 32 + 127) / 128);
             if (b.window == 1)
-                k_build_level<true, 1><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m,
+                k_build_level<true, 1><<<g, 128, 0, s>>>(b.recs, nall, b.V, b.node[(d + 1) & 1], b.node[d & 1], m,
                     d, b.status, b.count_filter);
             else
-                k_build_level<true><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
+                k_build_level<true><<<g, 128, 0, s>>>(b.recs, nall, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
                     b.status, b.count_filter);
         }
         else
         {
             const unsigned g = (unsigned)((nodes + 127) / 128);
-            k_build_level<false><<<g, 128, 0, s>>>(b.recs, nrec, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
+            k_build_level<false><<<g, 128, 0, s>>>(b.recs, nall, b.V, b.node[(d + 1) & 1], b.node[d & 1], m, d,
                 b.status, b.count_filter);
         }
         ++launch_counter();
@@ -354,7 +574,7 @@ __global__ void k_tri_write(const Rec* __restrict__ R, int nrec, const uint8_t* 
 
 void launch_extract(const BuildBuffers& b, int m, cudaStream_t s)
 {
-    const int      nrec = 3 * m;
+    const int      nrec = b.split.depth >= 0 ? 3 * m + b.split.spare : 3 * m;
     const unsigned g = (unsigned)((nrec + 255) / 256);
     k_tri_mask<<<g, 256, 0, s>>>(b.recs, nrec, b.tri_mask, b.status, b.count_filter);
     ++launch_counter();

@@ -210,6 +210,93 @@ def test_side_prefetch_same_result(lib):
             assert _digest(O.canonical(ref_tris).astype(np.int64)) == spec["serial"]["tri_digest"]
 
 
+def _split_inputs():
+    """Workloads for the two-walker merges: general position, clusters,
+    heavy ties (lattice, snapped grid), cocircular and near-collinear points,
+    and long seams (points on two lines parallel to the root's cut)."""
+    rng = np.random.default_rng(97)
+    n = 300000
+    yield "gauss", W.gaussian_mixture(400000, 64, 94)
+    yield "lattice", W.lattice_with_duplicates(400, 0.01, 95)
+    yield "circle", W.unit_circle(70000, 96)
+    yield "line", W.noisy_line(n, 97)
+    yield "skewed", np.column_stack([rng.exponential(1.0, n) ** 3, rng.standard_normal(n)])
+    yield "snapped", np.round(rng.random((n, 2)) * 256.0) / 256.0
+    centers = rng.random((40, 2))
+    yield "blobs", centers[rng.integers(0, 40, n)] + 1e-6 * rng.standard_normal((n, 2))
+    y = rng.random(n)
+    yield "two_lines", np.column_stack([np.where(np.arange(n) % 2 == 0, 0.25, 0.75) + 1e-9 * rng.random(n), y])
+
+
+def test_split_merges_same_result(lib):
+    """The top merges with two walkers (rising and mirrored falling, meeting
+    on the seam) give the canonical triangle set and representatives of the
+    one-walker build on every kind of input, without falling back (the
+    fallback would hide a wrong walk); two runs give identical arrays; the
+    1M uniform workload keeps the reference's digest. The merge window is
+    fixed at 2, so that lattice-like input (where a call leaves the split
+    merges off by default) runs them too."""
+    spec = next(s for s in _DIGESTS if s["name"] == "uniform_1m")
+    inputs = [("uniform_1m", C.make_large(spec))] + list(_split_inputs())
+    for name, p in inputs:
+        out = {}
+        for split in (True, False, True):
+            with G.Triangulation(lib) as t:
+                assert t.set_merge_window(2)
+                if not split:
+                    assert t.set_split_merges(-1)
+                assert t.execute(p) == 0, name
+                info = t.run_info()
+                if split:
+                    assert info["split_depth"] >= 0, name
+                    assert info["split_rerun"] == 0, name
+                else:
+                    assert info["split_depth"] == -1, name
+                out.setdefault(split, []).append((t.triangles_array().copy(), t.rep_array().copy()))
+        (t1, r1), (t2, r2) = out[True]
+        assert np.array_equal(t1, t2) and np.array_equal(r1, r2), name
+        t0, r0 = out[False][0]
+        assert np.array_equal(O.canonical(t1), O.canonical(t0)), name
+        assert np.array_equal(r1, r0), name
+        if name == "uniform_1m":
+            assert _digest(O.canonical(t1).astype(np.int64)) == spec["serial"]["tri_digest"]
+
+
+def test_split_merges_off_on_lattice_like_input(lib):
+    """On lattice-like input (most points share their x with another) a call
+    runs every merge with one walker, unless the merge window is fixed."""
+    p = W.lattice_with_duplicates(400, 0.01, 99)
+    with G.Triangulation(lib) as t:
+        assert t.execute(p) == 0
+        assert t.run_info()["split_depth"] == -1
+        ref = O.canonical(t.triangles_array())
+        assert t.set_merge_window(2)
+        assert t.execute(p) == 0
+        assert t.run_info()["split_depth"] >= 0
+        assert np.array_equal(O.canonical(t.triangles_array()), ref)
+
+
+def test_split_merges_knob(lib):
+    """qdtg_set_split_merges: depth -1..9 and at least 4,096 points accepted,
+    anything else refused; deeper splits and smaller nodes give the same
+    triangles."""
+    p = W.uniform(200000, 98)
+    with G.Triangulation(lib) as t:
+        assert not t.set_split_merges(10)
+        assert not t.set_split_merges(-2)
+        assert not t.set_split_merges(3, 4095)
+        assert t.set_split_merges(-1)
+        assert t.execute(p) == 0
+        ref = O.canonical(t.triangles_array())
+        for depth, mn in ((0, 4096), (5, 4096), (9, 4096), (8, 65536)):
+            assert t.set_split_merges(depth, mn)
+            assert t.execute(p) == 0
+            info = t.run_info()
+            assert info["split_rerun"] == 0
+            assert info["split_depth"] == min(depth, int(np.floor(np.log2(200000 / mn)))), (depth, mn)
+            assert np.array_equal(O.canonical(t.triangles_array()), ref), (depth, mn)
+
+
 def test_filter_stats_per_stage(lib):
     """Counting the predicates (per stage: leaves, thread merges, warp
     merges, extraction) leaves the result unchanged; every stage is counted;
