@@ -83,12 +83,12 @@ QDT_API int qdtg_set_split_tail(qdt_t* ptr, int on);
 QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
 
 /* The merges at the top of the build -- depths 0..max_depth (at most 9)
-   whose nodes hold at least min_points points (at least 4,096) -- run with
+   whose nodes hold at least min_points points (at least 256) -- run with
    two walkers each: the reference's rising merge from the lower common
    tangent and its mirror image from the upper one, which meet at a point of
    the seam. A merge whose falling walker meets cocircular or collinear
    points is finished by the rising one, so the triangulation is the same
-   as with one walker per merge (max_depth -1). Defaults 7 and 8,192.
+   as with one walker per merge (max_depth -1). Defaults 7 and 1,024.
    Returns 1, or 0 for a NULL context, values out of range or no usable
    GPU. No counterpart in the reference, whose merges are sequential. */
 QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
@@ -362,6 +362,7 @@ QDT_API void qdtg_batch_set_options(qdtg_batch* b, int count_filter_failures, in
    launch has at most warp_nodes nodes (default 4096). Returns 1, or 0 for a
    NULL batch or a negative value. */
 QDT_API int qdtg_batch_set_warp_nodes(qdtg_batch* b, int warp_nodes);
+
 /* The largest subtree (points, 4..1024; 0 = none) built in shared memory,
    as qdtg_set_cell_points(). Returns 1, or 0 for a bad value. */
 QDT_API int   qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points);

@@ -98,9 +98,9 @@ constexpr int kSeamDepth = 10;
 // Split merges (seam_split.cuh): at most these depths (their children's cuts
 // are recorded), nodes of at least kSplitFloor points.
 constexpr int kSplitMaxDepth = 9;
-constexpr int kSplitFloor = 4096;
+constexpr int kSplitFloor = 256;
 constexpr int kSplitDefaultDepth = 7;
-constexpr int kSplitDefaultPoints = 8192;
+constexpr int kSplitDefaultPoints = 1024;
 // bins of the records near a split merge's seam, along it (where its two
 // walkers meet)
 constexpr int kSeamBins = 64;

@@ -277,23 +277,23 @@ def test_split_merges_off_on_lattice_like_input(lib):
 
 
 def test_split_merges_knob(lib):
-    """qdtg_set_split_merges: depth -1..9 and at least 4,096 points accepted,
+    """qdtg_set_split_merges: depth -1..9 and at least 256 points accepted,
     anything else refused; deeper splits and smaller nodes give the same
     triangles."""
     p = W.uniform(200000, 98)
     with G.Triangulation(lib) as t:
         assert not t.set_split_merges(10)
         assert not t.set_split_merges(-2)
-        assert not t.set_split_merges(3, 4095)
+        assert not t.set_split_merges(3, 255)
         assert t.set_split_merges(-1)
         assert t.execute(p) == 0
         ref = O.canonical(t.triangles_array())
-        for depth, mn in ((0, 4096), (5, 4096), (9, 4096), (8, 65536)):
+        for depth, mn in ((0, 4096), (5, 4096), (9, 4096), (8, 65536), (9, 256)):
             assert t.set_split_merges(depth, mn)
             assert t.execute(p) == 0
             info = t.run_info()
             assert info["split_rerun"] == 0
-            assert info["split_depth"] == min(depth, int(np.floor(np.log2(200000 / mn)))), (depth, mn)
+            assert info["split_depth"] == min(depth, int(np.floor(np.log2(200000 / mn))), 9), (depth, mn)
             assert np.array_equal(O.canonical(t.triangles_array()), ref), (depth, mn)
 
 
