@@ -363,6 +363,15 @@ QDT_API void qdtg_batch_set_options(qdtg_batch* b, int count_filter_failures, in
    NULL batch or a negative value. */
 QDT_API int qdtg_batch_set_warp_nodes(qdtg_batch* b, int warp_nodes);
 
+/* The build of every set's tree as one persistent launch (on != 0): warps
+   of blocks resident on every SM take work units (32 small nodes, or one
+   large node) from a device counter, heights in increasing order, and a
+   merge waits (bounded) for its children's done flags instead of for the
+   end of a launch per height (the default, on == 0; faster on large
+   batches). A batch with shared-memory cells runs per height. The result
+   is the same. Returns 1, or 0 for a NULL batch or no usable GPU. No
+   counterpart in the reference, which builds sets on host threads. */
+QDT_API int qdtg_batch_set_persistent(qdtg_batch* b, int on);
 /* The largest subtree (points, 4..1024; 0 = none) built in shared memory,
    as qdtg_set_cell_points(). Returns 1, or 0 for a bad value. */
 QDT_API int   qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points);

@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqdt_gb300.so")
 
 GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_window", "qdtg_set_graphs", "qdtg_set_warp_nodes",
                "qdtg_set_defaults",
-               "qdtg_batch_set_warp_nodes", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
+               "qdtg_batch_set_warp_nodes", "qdtg_batch_set_persistent", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints", "qdtg_set_workspace_limit", "qdtg_context_workspace_bytes",
                "qdtg_set_split_tail", "qdtg_get_filter_stats", "qdtg_batch_get_filter_stats", "qdtg_set_side_prefetch", "qdtg_set_triangulation", "qdtg_set_split_merges",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
@@ -183,6 +183,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             ("qdtg_batch_set_options", [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], None),
             ("qdtg_batch_set_cell_points", [P, ctypes.c_int], ctypes.c_int),
             ("qdtg_batch_set_warp_nodes", [P, ctypes.c_int], ctypes.c_int),
+            ("qdtg_batch_set_persistent", [P, ctypes.c_int], ctypes.c_int),
             ("qdtg_batch_reserve", [P, S, S], ctypes.c_int),
             ("qdtg_batch_workspace_bytes", [P], S),
             ("qdtg_batch_get_run_info", [P, ctypes.POINTER(RunInfo)], ctypes.c_int),
@@ -453,6 +454,11 @@ class Batch:
 
     def set_warp_nodes(self, nodes: int) -> bool:
         return self.lib.qdtg_batch_set_warp_nodes(self.ptr, int(nodes)) == 1
+
+    def set_persistent(self, on: bool) -> bool:
+        """The build of every set's tree as one persistent launch (on) or one
+        launch per node height (off, the default)."""
+        return self.lib.qdtg_batch_set_persistent(self.ptr, int(bool(on))) == 1
 
     def stream(self) -> int:
         return self.lib.qdtg_batch_stream(self.ptr) or 0

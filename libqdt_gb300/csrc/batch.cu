@@ -25,6 +25,7 @@
 
 #include <cuda_runtime.h>
 
+#include "batch_kernels.hpp"
 #include "builder.cuh"
 #include "common.cuh"
 #include "context.hpp"
@@ -53,19 +54,6 @@ __device__ __forceinline__ uint64_t bkey(double v)
     if (v == 0.0) return 0x8000000000000000ull;
     const uint64_t b = (uint64_t)__double_as_longlong(v);
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-
-// the set of an element, from the offsets (binary search)
-__device__ __forceinline__ uint32_t find_set(const uint32_t* __restrict__ off, int S, uint32_t i)
-{
-    int lo = 0, hi = S;   // off[lo] <= i < off[hi]
-    while (hi - lo > 1)
-    {
-        const int mid = (lo + hi) >> 1;
-        if (off[mid] <= i) lo = mid;
-        else hi = mid;
-    }
-    return (uint32_t)lo;
 }
 
 __global__ void k_bkeys(const double2* __restrict__ pts, uint32_t n, const uint32_t* __restrict__ in_off, int S,
@@ -343,159 +331,6 @@ __global__ void k_bfinalize(const uint32_t* __restrict__ A, const uint32_t* __re
     vid[i] = uid[u];
 }
 
-// All nodes of one height (the levels below them) in every participating
-// set. Nodes of equal height have sizes within a factor of two, so the
-// merges of a launch are alike, whatever the sizes of their sets; a node's
-// children have smaller heights and were built by earlier launches. A node
-// of height h lies at depth D - h (D the set's split depth) or, when it is a
-// smaller sibling, at D - h - 1: the launch runs over entries (set, depth)
-// with 2^depth slots each (entry e covers slots [eoff[e], eoff[e + 1])) and
-// skips the slots whose node has another height. The single-set
-// k_build_level is the same body with depth-synchronous launches (there all
-// nodes of a depth are alike).
-template <bool WARP, bool LEAF>
-__global__ void QDTG_BUILD_BOUNDS(WARP) k_bbuild_height(Rec* __restrict__ R, int nrec,
-    const double2* __restrict__ V, NodeOut* __restrict__ nodes, const uint32_t* __restrict__ noff,
-    const uint32_t* __restrict__ ent, const uint32_t* __restrict__ eoff, int nent, const uint32_t* __restrict__ u_off,
-    int h, DevStatus* st, int count)
-{
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long flat = WARP ? (g >> 5) : g;
-    const int       lane = WARP ? (int)(threadIdx.x & 31) : 0;
-    if (flat >= (long long)eoff[nent]) return;
-    unsigned flags = *(volatile unsigned*)&st->flags;
-    if (WARP) flags = __shfl_sync(0xffffffffu, flags, 0);
-    if (flags & kFatal) return;
-    const uint32_t  e = find_set(eoff, nent, (uint32_t)flat);
-    const uint32_t  s = ent[e] >> 5;
-    const int       d = (int)(ent[e] & 31u);
-    const long long k = flat - eoff[e];
-    const int       base = (int)u_off[s], ms = (int)(u_off[s + 1] - u_off[s]);
-    int             lo, hi;
-    if (!node_range(ms, d, k, lo, hi) || subtree_levels(hi - lo) != h) return;
-    lo += base;
-    hi += base;
-    NodeOut* const out = nodes + noff[s];   // heap order: (1 << depth) + index
-    const int      n = hi - lo;
-    Builder        B{ R, nrec, st,
-        pred_stage(st, (LEAF || n <= 3) ? kStageLeaf : (WARP ? kStageWarp : kStageThread), count), -1, -1, false };
-    NodeOut        o;
-    // height 0 is all leaves, the other heights all merges: two kernels, so
-    // that neither carries the other's code
-    o.le2 = o.re2 = -1;
-    o.pad0 = o.pad1 = 0;
-    if (LEAF || n <= 3)
-    {
-        if (!LEAF || lane != 0) return;
-        B.leaf(lo, hi, V, o.le, o.re);
-        if (d > 0 && !B.bad) extremes_by_walk(B, o.le, o.re, d & 1, 8, o.le2, o.re2);
-    }
-    else
-    {
-        const NodeOut L = out[(2ll << d) + 2 * k], Rn = out[(2ll << d) + 2 * k + 1];
-        if ((L.fhead >= 0 && (L.ftail < 3 * lo || L.ftail >= 3 * hi)) ||
-            (Rn.fhead >= 0 && (Rn.ftail < 3 * lo || Rn.ftail >= 3 * hi)))
-        {
-            if (lane == 0) B.fail(ST_BAD_INDEX);
-            return;
-        }
-        if (L.fhead >= 0)
-        {
-            B.fhead = L.fhead;
-            if (Rn.fhead >= 0)
-            {
-                if (lane == 0) R[L.ftail].link = Rn.fhead;
-                B.ftail = Rn.ftail;
-            }
-            else
-                B.ftail = L.ftail;
-        }
-        else
-        {
-            B.fhead = Rn.fhead;
-            B.ftail = Rn.ftail;
-        }
-        const int lim = 8 * n + 64;
-        const int g = (d - 1) & 1;   // the parent's frame
-        int       rl = 0, rr = 0;
-        NodeOut*      self = &out[(1ll << d) + k];
-        volatile int* first = nullptr;
-        if (d > 0 && lane == 0)
-        {
-            extremes_before_merge(R, nrec, st, &out[(2ll << d) + 2 * k], &out[(2ll << d) + 2 * k + 1], self, g);
-            first = lower_tangent_slot(self);
-        }
-        if (WARP) warp_merge(B, L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
-        else B.merge(L.le, L.re, Rn.le, Rn.re, lim, rl, rr, first);
-        if (lane != 0) return;
-        o.le2 = rl;
-        o.re2 = rr;
-        if (d > 0 && !B.bad)
-        {
-            const int2 x = extremes_after_merge(R, nrec, st, B.basel_last, self, &out[(2ll << d) + 2 * k],
-                &out[(2ll << d) + 2 * k + 1], g, n + 8);
-            rl = x.x;
-            rr = x.y;
-        }
-        o.le = rl;
-        o.re = rr;
-    }
-    B.settle_tail();
-    o.fhead = B.fhead;
-    o.ftail = B.ftail;
-    out[(1ll << d) + k] = o;
-}
-
-// The cells of every set, one warp each: cell g belongs to the set s with
-// cell_off[s] <= g < cell_off[s + 1] and is node g - cell_off[s] of the set's
-// cell depth.
-__global__ void __launch_bounds__(kCellBlockWarps * 32) k_bbuild_cells(Rec* __restrict__ R,
-    const double2* __restrict__ V, NodeOut* __restrict__ nodes, const uint32_t* __restrict__ noff,
-    const uint32_t* __restrict__ cell_off, int S, const uint32_t* __restrict__ u_off, int C, uint32_t ncells,
-    DevStatus* st, int count)
-{
-    extern __shared__ __align__(16) char bcell_smem[];
-    const int      w = threadIdx.x >> 5;
-    const uint32_t g = blockIdx.x * (blockDim.x >> 5) + w;
-    if (g >= ncells) return;
-    const unsigned flags = __shfl_sync(0xffffffffu, *(volatile unsigned*)&st->flags, 0);
-    if (flags & kFatal) return;
-    const uint32_t  s = find_set(cell_off, S, g);
-    const int       base = (int)u_off[s], ms = (int)(u_off[s + 1] - u_off[s]);
-    const int       dc = cell_depth(ms, C);
-    const long long k = (long long)(g - cell_off[s]);
-    int             lo, hi;
-    if (!node_range(ms, dc, k, lo, hi) || hi - lo > C) return;
-    build_cell(bcell_smem + w * cell_smem_bytes(C), V, R, base + lo, base + hi, dc, st, pred_stage(st, kStageThread, count),
-        nodes + noff[s] + (1ll << dc) + k);
-}
-
-// extraction; records of sets that were not built are skipped
-__global__ void k_btri_mask(const Rec* __restrict__ R, int nrec, const uint32_t* __restrict__ useg,
-    const uint8_t* __restrict__ skip, uint8_t* __restrict__ mask, DevStatus* st, int count)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nrec) return;
-    if ((*(volatile unsigned*)&st->flags & kFatal) || skip[useg[k / 3]])
-    {
-        mask[k] = 0;
-        return;
-    }
-    Builder B{ const_cast<Rec*>(R), nrec, st, pred_stage(st, kStageExtract, count), -1, -1, false };
-    uint8_t mk = 0;
-    if (R[k].org[0] >= 0)
-    {
-        for (int s = 0; s < 2; ++s)
-        {
-            const int e = 2 * k + s;
-            const int f = B.lnext(e), g = B.lnext(f);
-            if (B.lnext(g) != e) continue;
-            if (e > f || e > g) continue;
-            if (ccw(B.porg(e), B.porg(f), B.porg(g), B.pc)) mk |= (uint8_t)(1 << s);
-        }
-    }
-    mask[k] = B.bad ? 0 : mk;
-}
 
 struct BMaskCount
 {
@@ -589,6 +424,12 @@ struct BatchEngine
     int                   warp_min_points = 512;   // heights whose nodes have at least this many points: a warp per node
     int                   warp_nodes = 4096;       // heights with at most this many nodes: a warp per node
     int                   cell_points = 0;         // largest cell built in shared memory (0: none)
+    bool                  persistent = false;      // the build as one persistent launch (k_bbuild_persist)
+    uint32_t*             done = nullptr;          // per node slot: set once the node is built (persistent form)
+    uint32_t*             pcounter = nullptr;      // the persistent form's unit counter
+    PersistPlan*          plan = nullptr;          // its schedule (device copy of h_plan)
+    PersistPlan           h_plan{};
+    int                   persist_grid = 0;        // its resident blocks
     std::vector<uint32_t> h_cell_off;
     uint32_t              ncells = 0;
     cudaEvent_t           ev[8] = {};
@@ -625,7 +466,13 @@ struct BatchEngine
     {
         return h >= 1 && (3ll * (1ll << (h - 1)) + 1 >= warp_min_points || nodes <= warp_nodes);
     }
-    void post_sync_work(size_t N, size_t S, uint32_t M, int Dmax);
+    void post_sync_work(size_t N, size_t S, uint32_t M, int Dmax, bool wide);
+    // this batch's build as one persistent launch (not with cells)
+    bool persist_now() const
+    {
+        return persistent && persist_grid > 0 && !(cell_points > 0 && ncells > 0) &&
+               (int)h_nent.size() <= kMaxHeights;
+    }
 };
 
 namespace {
@@ -688,6 +535,9 @@ size_t bcarve(BatchEngine& g, char* base, size_t N, size_t S)
     // node heaps: sum over sets of 2^(D+1) <= 4 N + 2 S
     g.nodes_cap = 4 * N + 2 * S + 16;
     g.nodes = c.take<NodeOut>(g.nodes_cap);
+    g.done = c.take<uint32_t>(g.nodes_cap);
+    g.pcounter = c.take<uint32_t>(8);
+    g.plan = c.take<PersistPlan>(1);
     // split tails: a set of m points has 2^tail_depth(m) < 2 m / kTailMax
     // tail nodes when it has more than one
     g.tail_cap = S + 2 * N / kTailMax + 16;
@@ -736,9 +586,11 @@ int BatchEngine::ensure(size_t N, size_t S)
 // Everything after the distinct counts are known: frames, split levels,
 // finalize, build, extraction. Shapes depend on the counts only, so the
 // launches can be recorded once per shape.
-void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax)
+void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax, bool wide)
 {
     cudaStream_t s = stream;
+    // the flags and predicate counters of a first pass of the same batch
+    cudaMemsetAsync(status, 0, sizeof(DevStatus), s);
     const int    segp = S <= 1 ? 0 : (S <= 256 ? 1 : (S <= 65536 ? 2 : 3));
     // frames
     k_useg<<<gridn(M, 256), 256, 0, s>>>(u_off, (int)S, M, useg);
@@ -803,38 +655,64 @@ void BatchEngine::post_sync_work(size_t N, size_t S, uint32_t M, int Dmax)
     ++launch_counter();
     if (timing) cudaEventRecord(ev[4], s);
     const int nrec = 3 * (int)M;
+    BatchBuildArgs a;
+    a.recs = recs;
+    a.nrec = nrec;
+    a.V = V;
+    a.nodes = nodes;
+    a.noff = noff;
+    a.ents = ents;
+    a.eoffs = eoffs;
+    a.u_off = u_off;
+    a.cell_off = cell_off;
+    a.S = (int)S;
+    a.cell_points = cell_points;
+    a.ncells = ncells;
+    a.status = status;
+    a.count = count_filter ? 1 : 0;
+    a.counter = pcounter;
+    a.done = done;
+    a.useg = useg;
+    a.skip = skip;
+    a.mask = mask;
     // the bottom of every set's tree in shared-memory cells
     if (cell_points > 0 && ncells > 0)
     {
-        const int warps = cell_block_warps(cell_points);
-        k_bbuild_cells<<<(ncells + warps - 1) / warps, warps * 32, warps * cell_smem_bytes(cell_points), s>>>(recs, V,
-            nodes, noff, cell_off, (int)S, u_off, cell_points, ncells, status, count_filter ? 1 : 0);
+        if (wide) wide::launch_bbuild_cells(a, s);
+        else narrow::launch_bbuild_cells(a, s);
         ++launch_counter();
     }
     // the nodes above: one launch per height, from the leaves up; a warp per
     // node for the heights whose nodes have at least warp_min_points points
-    for (int h = 0; h < (int)h_nent.size(); ++h)
+    // -- or all heights in one persistent launch
+    if (persist_now())
     {
-        const int nent = h_nent[h];
-        if (nent == 0) continue;
-        const long long slots = h_eoffs[h_eoff0[h] + nent];
-        if (slots == 0) continue;
-        const uint32_t* en = ents + h_ent0[h];
-        const uint32_t* eo = eoffs + h_eoff0[h];
-        const int cf = count_filter ? 1 : 0;
-        if (h == 0)
-            k_bbuild_height<false, true><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes, noff,
-                en, eo, nent, u_off, h, status, cf);
-        else if (height_warp(h, slots))
-            k_bbuild_height<true, false><<<(unsigned)((slots * 32 + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes,
-                noff, en, eo, nent, u_off, h, status, cf);
-        else
-            k_bbuild_height<false, false><<<(unsigned)((slots + 127) / 128), 128, 0, s>>>(recs, nrec, V, nodes, noff,
-                en, eo, nent, u_off, h, status, cf);
+        cudaMemsetAsync(done, 0, (size_t)h_noff[S] * sizeof(uint32_t), s);
+        cudaMemsetAsync(pcounter, 0, sizeof(uint32_t), s);
+        // (mostly thread-per-node merges: the build with the widest tier)
+        wide::launch_bbuild_persist(a, plan, persist_grid, s);
         ++launch_counter();
     }
+    else
+        for (int h = 0; h < (int)h_nent.size(); ++h)
+        {
+            const int nent = h_nent[h];
+            if (nent == 0) continue;
+            const long long slots = h_eoffs[h_eoff0[h] + nent];
+            if (slots == 0) continue;
+            const uint32_t* en = ents + h_ent0[h];
+            const uint32_t* eo = eoffs + h_eoff0[h];
+            const bool      w = height_warp(h, slots);
+            // the thread-per-node merges always from the build with the
+            // widest tier: measured twice as fast as the build without it
+            // (same instructions, a quarter of the waits on loads)
+            if (wide || (h > 0 && !w)) wide::launch_bbuild_height(a, h, en, eo, nent, slots, w, s);
+            else narrow::launch_bbuild_height(a, h, en, eo, nent, slots, w, s);
+            ++launch_counter();
+        }
     if (timing) cudaEventRecord(ev[5], s);
-    k_btri_mask<<<gridn(nrec, 256), 256, 0, s>>>(recs, nrec, useg, skip, mask, status, count_filter ? 1 : 0);
+    if (wide) wide::launch_btri_mask(a, s);
+    else narrow::launch_btri_mask(a, s);
     ++launch_counter();
     scan_exclusive(BMaskCount{ mask }, (size_t)nrec, tri_off, scratch, words + 1, s);
     k_btri_write<<<gridn(nrec, 256), 256, 0, s>>>(recs, nrec, mask, tri_off, vid, useg, in_off, tris);
@@ -990,76 +868,105 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
     cudaMemcpyAsync(cell_off, h_cell_off.data(), (S + 1) * 4, cudaMemcpyHostToDevice, s);
     if (!h_ents.empty()) cudaMemcpyAsync(ents, h_ents.data(), h_ents.size() * 4, cudaMemcpyHostToDevice, s);
     if (!h_eoffs.empty()) cudaMemcpyAsync(eoffs, h_eoffs.data(), h_eoffs.size() * 4, cudaMemcpyHostToDevice, s);
-    if (C > 0)
-        cudaFuncSetAttribute(k_bbuild_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
-            cell_block_warps(C) * cell_smem_bytes(C));
+    if (persist_now())
+    {
+        // the persistent build's units, heights in increasing order
+        h_plan = PersistPlan{};
+        h_plan.nh = (int)h_nent.size();
+        uint64_t units = 0;
+        for (int h = 0; h < h_plan.nh; ++h)
+        {
+            const long long slots = h_nent[h] ? h_eoffs[h_eoff0[h] + h_nent[h]] : 0;
+            h_plan.unit_off[h] = (uint32_t)units;
+            h_plan.ent0[h] = (uint32_t)h_ent0[h];
+            h_plan.eoff0[h] = (uint32_t)h_eoff0[h];
+            h_plan.nent[h] = h_nent[h];
+            h_plan.warp[h] = height_warp(h, slots) ? 1 : 0;
+            units += (uint64_t)(h_plan.warp[h] ? slots : (slots + 31) / 32);
+        }
+        if (units > 0xFFFFFFFFull) return QDT_ERR_INTERNAL;
+        h_plan.unit_off[h_plan.nh] = (uint32_t)units;
+        cudaMemcpyAsync(plan, &h_plan, sizeof(PersistPlan), cudaMemcpyHostToDevice, s);
+    }
 
     // the post-synchronisation launches, replayed from a graph per shape
-    bool ran = false;
-    if (use_graph && !timing)
-    {
-        std::vector<uint32_t> shape;
-        shape.reserve(2 * S + 8);
-        shape.insert(shape.end(), { (uint32_t)N, (uint32_t)((uint64_t)N >> 32), (uint32_t)S, count_filter ? 1u : 0u,
-                                      (uint32_t)warp_min_points, (uint32_t)warp_nodes, (uint32_t)cell_points });
-        shape.insert(shape.end(), h_u_off.begin(), h_u_off.begin() + S + 1);
-        shape.insert(shape.end(), skipv.begin(), skipv.end());
-        uint64_t key = 1469598103934665603ull;
-        for (uint32_t v : shape) key = (key ^ v) * 1099511628211ull;
-        auto it = graphs.find(key);
-        if (it != graphs.end() && it->second.shape != shape)
-            it = graphs.end();   // another shape with the same hash: launch by launch
-        else if (it == graphs.end() && graphs.size() < kMaxGraphs)
+    auto post = [&](bool wide) {
+        bool ran = false;
+        if (use_graph && !timing)
         {
-            cudaGraph_t graph = nullptr;
-            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
+            std::vector<uint32_t> shape;
+            shape.reserve(2 * S + 9);
+            shape.insert(shape.end(), { (uint32_t)N, (uint32_t)((uint64_t)N >> 32), (uint32_t)S,
+                                          count_filter ? 1u : 0u, (uint32_t)warp_min_points, (uint32_t)warp_nodes,
+                                          (uint32_t)cell_points, persistent ? 1u : 0u, wide ? 1u : 0u });
+            shape.insert(shape.end(), h_u_off.begin(), h_u_off.begin() + S + 1);
+            shape.insert(shape.end(), skipv.begin(), skipv.end());
+            uint64_t key = 1469598103934665603ull;
+            for (uint32_t v : shape) key = (key ^ v) * 1099511628211ull;
+            auto it = graphs.find(key);
+            if (it != graphs.end() && it->second.shape != shape)
+                it = graphs.end();   // another shape with the same hash: launch by launch
+            else if (it == graphs.end() && graphs.size() < kMaxGraphs)
             {
-                const int before = launch_counter();
-                post_sync_work(N, S, M, Dmax);
-                const int added = launch_counter() - before;
-                if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
                 {
-                    cudaGraphExec_t exec = nullptr;
-                    if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
-                        it = graphs.emplace(key, GraphEntry{ exec, added, std::move(shape) }).first;
-                    cudaGraphDestroy(graph);
+                    const int before = launch_counter();
+                    post_sync_work(N, S, M, Dmax, wide);
+                    const int added = launch_counter() - before;
+                    if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
+                    {
+                        cudaGraphExec_t exec = nullptr;
+                        if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                            it = graphs.emplace(key, GraphEntry{ exec, added, std::move(shape) }).first;
+                        cudaGraphDestroy(graph);
+                    }
+                    cudaGetLastError();
+                    launch_counter() = before;   // nothing ran during the capture
                 }
-                cudaGetLastError();
-                launch_counter() = before;   // nothing ran during the capture
+                else
+                    cudaGetLastError();
             }
-            else
-                cudaGetLastError();
-        }
-        if (it != graphs.end())
-        {
-            if (cudaGraphLaunch(it->second.exec, s) == cudaSuccess)
+            if (it != graphs.end())
             {
-                ran = true;
-                launch_counter() += it->second.launches;   // the kernels recorded in the graph
+                if (cudaGraphLaunch(it->second.exec, s) == cudaSuccess)
+                {
+                    ran = true;
+                    launch_counter() += it->second.launches;   // the kernels recorded in the graph
+                }
+                else
+                    cudaGetLastError();
             }
-            else
-                cudaGetLastError();
         }
-    }
-    if (!ran) post_sync_work(N, S, M, Dmax);
-    if (timing) cudaEventRecord(ev[6], s);
-    cudaMemcpyAsync(h_status, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(h_words, words, 8 * 4, cudaMemcpyDeviceToHost, s);
-    h_tri_base.resize(S + 1);
-    cudaMemcpyAsync(h_tri_base.data(), tri_base, (S + 1) * 4, cudaMemcpyDeviceToHost, s);
-    if (host_io)
-    {
-        // the count is at most 2 M: copy that bound, not a round trip
-        h_tris.resize(6 * (size_t)M + 3);
-        h_rep.resize(N);
-        if (M) cudaMemcpyAsync(h_tris.data(), tris, 6 * (size_t)M * 4, cudaMemcpyDeviceToHost, s);
-        if (N) cudaMemcpyAsync(h_rep.data(), rep, N * 4, cudaMemcpyDeviceToHost, s);
-    }
-    if (timing) cudaEventRecord(ev[7], s);
-    if (cudaStreamSynchronize(s) != cudaSuccess)
-    {
+        if (!ran) post_sync_work(N, S, M, Dmax, wide);
+        if (timing) cudaEventRecord(ev[6], s);
+        cudaMemcpyAsync(h_status, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(h_words, words, 8 * 4, cudaMemcpyDeviceToHost, s);
+        h_tri_base.resize(S + 1);
+        cudaMemcpyAsync(h_tri_base.data(), tri_base, (S + 1) * 4, cudaMemcpyDeviceToHost, s);
+        if (host_io)
+        {
+            // the count is at most 2 M: copy that bound, not a round trip
+            h_tris.resize(6 * (size_t)M + 3);
+            h_rep.resize(N);
+            if (M) cudaMemcpyAsync(h_tris.data(), tris, 6 * (size_t)M * 4, cudaMemcpyDeviceToHost, s);
+            if (N) cudaMemcpyAsync(h_rep.data(), rep, N * 4, cudaMemcpyDeviceToHost, s);
+        }
+        if (timing) cudaEventRecord(ev[7], s);
+        if (cudaStreamSynchronize(s) == cudaSuccess) return true;
         cudaGetLastError();
-        return QDT_ERR_INTERNAL;
+        return false;
+    };
+    if (!post(false)) return QDT_ERR_INTERNAL;
+    bool need_wide = false;
+    for (int sg = 0; sg < kPredStages; ++sg) need_wide = need_wide || h_status->pc[sg].wide;
+    if (need_wide)
+    {
+        // a predicate needed the widest exact tier, which the default
+        // kernels leave out: the stages after the synchronisation once more
+        // with the kernels that have it
+        info.wide = 1;
+        if (!post(true)) return QDT_ERR_INTERNAL;
     }
     ntri = h_words[1];
     info.ntri = ntri;
@@ -1329,6 +1236,31 @@ QDT_API int qdtg_batch_set_warp_nodes(qdtg_batch* b, int warp_nodes)
     return 1;
 }
 
+QDT_API int qdtg_batch_set_persistent(qdtg_batch* b, int on)
+{
+    if (!b) return 0;
+    if (on && b->e.persist_grid <= 0)
+    {
+        // as many blocks as are resident at once: the warps take their work
+        // from a counter, so further blocks would only wait for a slot
+        int dev = b->e.device, sms = 0, per = 0;
+        if (cudaSetDevice(dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                cudaSuccess ||
+            sms <= 0)
+        {
+            cudaGetLastError();
+            return 0;
+        }
+        // resident blocks of both variants (a batch may run again with the
+        // wide one)
+        per = std::min(qdtg::narrow::persist_blocks_per_sm(), qdtg::wide::persist_blocks_per_sm());
+        if (per <= 0) return 0;
+        b->e.persist_grid = sms * per;
+    }
+    b->e.persistent = on != 0;
+    return 1;
+}
+
 QDT_API int qdtg_batch_set_cell_points(qdtg_batch* b, int cell_points)
 {
     if (!b) return 0;
@@ -1368,6 +1300,7 @@ QDT_API int qdtg_batch_get_run_info(const qdtg_batch* b, qdtg_run_info* info)
     info->ms_total = r.ms.total;
     info->device_flags = r.device_status;
     info->kernel_launches = r.launches;
+    info->wide_exact = r.wide;
     return 1;
 }
 

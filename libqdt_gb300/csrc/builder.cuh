@@ -14,11 +14,13 @@
 #include <cstdio>
 #endif
 
-// Launch bounds of the level kernels: 128 threads. (A minimum of resident
-// blocks, which would cap the registers, measured no faster: the
-// thread-per-node levels are chains of dependent loads and predicates that
-// run in about one wave.)
-#define QDTG_BUILD_BOUNDS(WARP) __launch_bounds__(128)
+// Register cap of the level kernels (launched with 128 threads): 168, no
+// spills in any form. Without a cap ptxas gave the warp forms 128 registers
+// and 48-76 bytes of spills in the merge loop, which made the many-set
+// build's warp heights markedly slower. (A lower cap for more resident
+// blocks measured no faster: the thread-per-node levels are chains of
+// dependent loads and predicates that run in about one wave.)
+#define QDTG_BUILD_BOUNDS(WARP) __maxnreg__(168)
 
 namespace qdtg {
 

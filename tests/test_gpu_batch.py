@@ -183,3 +183,79 @@ def test_config_b_every_set_equals_reference(lib):
                 if got != want:
                     bad.append(i)
             assert not bad, (rep_call, bad[:10], len(bad))
+
+
+def test_persistent_build_same_result(lib):
+    """The build as one persistent launch (qdtg_batch_set_persistent: warps
+    take node units from a counter and wait for their children's done flags)
+    gives every set the oracle's result, like the launch per height: special
+    and uneven sets, graph replay, the thread form at every height and the
+    warp form at every height, a failing set among good ones, and back to the
+    launch per height in the same batch object."""
+    sets = special_sets() + W.many_sets(count=200, lo=16, hi=40000, seed=31)
+    with G.Batch(lib) as b:
+        assert b.execute_sets(sets) == Q.QDT_OK
+        per_height = b.run_info()["kernel_launches"]
+        assert b.set_persistent(True)
+        for _ in range(2):                                                # capture, then graph replay
+            assert b.execute_sets(sets) == Q.QDT_OK
+            check_batch(b, sets)
+            assert b.run_info()["device_flags"] == 0
+        assert b.run_info()["kernel_launches"] < per_height
+        for points, nodes in ((1 << 30, 0), (1 << 30, 1 << 30), (4, 0)):
+            b.set_options(warp_min_points=points)
+            assert b.set_warp_nodes(nodes)
+            assert b.execute_sets(sets) == Q.QDT_OK
+            check_batch(b, sets)
+        bad = [s.copy() for s in sets[-30:]]
+        bad[5][2, 1] = np.nan
+        assert b.execute_sets(bad) == Q.QDT_OK
+        assert b.status(5) == Q.QDT_ERR_NOT_FINITE
+        check_batch(b, bad)
+        assert b.set_persistent(False)
+        assert b.execute_sets(sets) == Q.QDT_OK
+        check_batch(b, sets)
+
+
+def test_persistent_build_one_large_set(lib):
+    """One set of 300,000 points and a few small ones in the persistent
+    form: the chain of waits runs from the leaves to a root that is merged
+    by one warp while most other warps have run out of work."""
+    sets = [W.uniform(300000, 33), W.uniform(100, 34), W.lattice_with_duplicates(40, 0.02, 35)]
+    with G.Batch(lib) as b:
+        assert b.set_persistent(True)
+        assert b.execute_sets(sets) == Q.QDT_OK
+        check_batch(b, sets)
+
+
+def test_batch_wide_exact_rerun(lib):
+    """A set whose coordinates span more than 95 bits inside one predicate
+    needs the widest exact tier. The batch's thread-per-node merges (and its
+    persistent build) come from the build that has it; its leaves, warp
+    merges and extraction come from the build without it, where such a
+    predicate flags the batch, which then runs its stages after the
+    synchronisation again with the kernels that have the tier (run_info
+    wide_exact). Every set -- that one and the ordinary ones beside it --
+    gets the oracle's result either way; ordinary batches never take the
+    second run."""
+    rng = np.random.default_rng(71)
+    base = rng.integers(0, 40, size=(3000, 2)).astype(np.float64)
+    tiny = base.copy()
+    tiny[::7] += np.ldexp(rng.integers(1, 8, size=(tiny[::7].shape[0], 2)).astype(np.float64), -90)
+    ordinary = W.many_sets(count=30, lo=16, hi=5000, seed=36)
+    mixed = ordinary[:10] + [tiny] + ordinary[10:]
+    with G.Batch(lib) as b:
+        assert b.execute_sets(ordinary) == Q.QDT_OK
+        assert b.run_info()["wide_exact"] == 0
+        check_batch(b, ordinary)
+        assert b.execute_sets(mixed) == Q.QDT_OK
+        check_batch(b, mixed)
+        # a warp per node at every height: the merges meet the tier in the
+        # build without it
+        b.set_options(warp_min_points=4)
+        assert b.execute_sets(mixed) == Q.QDT_OK
+        assert b.run_info()["wide_exact"] == 1
+        check_batch(b, mixed)
+        assert b.set_persistent(True)
+        assert b.execute_sets(mixed) == Q.QDT_OK
+        check_batch(b, mixed)
