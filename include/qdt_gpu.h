@@ -37,8 +37,9 @@ typedef struct qdtg_run_info
     int                wide_exact;      /* 1: a predicate needed the widest exact tier and the build ran
                                            again with the kernels that have it */
     int                split_depth;     /* deepest depth whose merges ran with two walkers (-1: none) */
-    int                split_rerun;     /* 1: a two-walker merge could not finish and the build ran
-                                           again with one walker per merge */
+    int                split_rerun;     /* 1: a split merge could not finish and the build ran again
+                                           (with one seam segment a merge, else one walker) */
+    int                split_segments;  /* the most seam segments of a split merge in the last pass */
 } qdtg_run_info;
 
 /* Options of a context: count_filter_failures != 0 counts the predicate calls
@@ -92,6 +93,18 @@ QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
    Returns 1, or 0 for a NULL context, values out of range or no usable
    GPU. No counterpart in the reference, whose merges are sequential. */
 QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
+
+/* Seam segments of one split merge at most (1..4, default 4; a node gets
+   one more segment per 65,536 points, on calls of at least 65,536 points).
+   Segments beyond the first begin at cross edges found before the merge:
+   pairs of mutually nearest vertices of the two halves, which are edges of
+   every Delaunay triangulation of the merged points; each segment is walked
+   by a rising and a falling walker. The triangulation is the same for
+   every value (a merge whose walkers above the first segment meet a
+   cocircular or collinear configuration runs again with one walker).
+   Returns 1, or 0 for a NULL context, a value out of range or no usable
+   GPU. No counterpart in the reference. */
+QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments);
 
 /* Caps the device bytes of the context's workspace (0: no cap, the
    default). A batch call whose workspace would exceed the cap returns

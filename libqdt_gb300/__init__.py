@@ -26,7 +26,7 @@ GPU_SYMBOLS = ("qdtg_set_options", "qdtg_set_cell_points", "qdtg_set_merge_windo
                "qdtg_set_defaults",
                "qdtg_batch_set_warp_nodes", "qdtg_batch_set_persistent", "qdtg_set_mesh_on_gpu", "qdtg_locate_points", "qdtg_insert_points",
                "qdtg_trace_constraints", "qdtg_set_workspace_limit", "qdtg_context_workspace_bytes",
-               "qdtg_set_split_tail", "qdtg_get_filter_stats", "qdtg_batch_get_filter_stats", "qdtg_set_side_prefetch", "qdtg_set_triangulation", "qdtg_set_split_merges",
+               "qdtg_set_split_tail", "qdtg_get_filter_stats", "qdtg_batch_get_filter_stats", "qdtg_set_side_prefetch", "qdtg_set_triangulation", "qdtg_set_split_merges", "qdtg_set_split_segments",
                "qdtg_get_defaults", "qdtg_device_name", "qdtg_get_run_info", "qdtg_execute_device", "qdtg_device_triangles",
                "qdtg_download_device_triangles",
                "qdtg_copy_triangles", "qdtg_copy_rep", "qdtg_stream", "qdtg_last_cuda_error", "qdtg_orient2d",
@@ -62,6 +62,7 @@ class RunInfo(ctypes.Structure):
         ("wide_exact", ctypes.c_int),
         ("split_depth", ctypes.c_int),
         ("split_rerun", ctypes.c_int),
+        ("split_segments", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -118,6 +119,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_side_prefetch.restype = ctypes.c_int
     lib.qdtg_set_split_merges.argtypes = [P, ctypes.c_int, ctypes.c_int]
     lib.qdtg_set_split_merges.restype = ctypes.c_int
+    lib.qdtg_set_split_segments.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_split_segments.restype = ctypes.c_int
     lib.qdtg_set_workspace_limit.argtypes = [P, ctypes.c_size_t]
     lib.qdtg_set_workspace_limit.restype = ctypes.c_int
     lib.qdtg_context_workspace_bytes.argtypes = [P]
@@ -266,6 +269,11 @@ class Triangulation(qdt_api.Context):
         """Two walkers per merge at depths 0..max_depth (nodes of at least
         min_points points); max_depth -1: one walker per merge."""
         return self.lib.qdtg_set_split_merges(self.ptr, int(max_depth), int(min_points)) == 1
+
+    def set_split_segments(self, max_segments: int) -> bool:
+        """Seam segments of one split merge at most (1..4): segments beyond
+        the first begin at cross edges found before the merge."""
+        return self.lib.qdtg_set_split_segments(self.ptr, int(max_segments)) == 1
 
     def filter_stats(self) -> dict:
         """Per-stage predicate statistics of the last batch call (counted

@@ -909,15 +909,19 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
             else if (it == graphs.end() && graphs.size() < kMaxGraphs)
             {
                 cudaGraph_t graph = nullptr;
+                cudaGetLastError();   // an error left by an earlier call is not this one's
                 if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
                 {
                     const int before = launch_counter();
                     post_sync_work(N, S, M, Dmax, wide);
-                    const int added = launch_counter() - before;
+                    // a launch refused while recording: no graph, the
+                    // launches run directly below and report it
+                    const bool recorded = cudaGetLastError() == cudaSuccess;
+                    const int  added = launch_counter() - before;
                     if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
                     {
                         cudaGraphExec_t exec = nullptr;
-                        if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                        if (recorded && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
                             it = graphs.emplace(key, GraphEntry{ exec, added, std::move(shape) }).first;
                         cudaGraphDestroy(graph);
                     }
@@ -938,7 +942,12 @@ int BatchEngine::run(size_t N, size_t S, bool host_io)
                     cudaGetLastError();
             }
         }
-        if (!ran) post_sync_work(N, S, M, Dmax, wide);
+        if (!ran)
+        {
+            cudaGetLastError();
+            post_sync_work(N, S, M, Dmax, wide);
+            if (cudaGetLastError() != cudaSuccess) return false;
+        }
         if (timing) cudaEventRecord(ev[6], s);
         cudaMemcpyAsync(h_status, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(h_words, words, 8 * 4, cudaMemcpyDeviceToHost, s);

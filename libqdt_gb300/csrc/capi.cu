@@ -572,6 +572,7 @@ QDT_API int qdtg_get_run_info(const qdt_t* ptr, qdtg_run_info* info)
     info->wide_exact = r.wide;
     info->split_depth = r.split_depth;
     info->split_rerun = r.split_rerun;
+    info->split_segments = r.split_segments;
     return 1;
 }
 
@@ -608,6 +609,15 @@ QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points)
     if (!c || max_depth < -1 || max_depth > qdtg::kSplitMaxDepth || min_points < qdtg::kSplitFloor) return 0;
     if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
     c->engine->set_split(max_depth, min_points);
+    return 1;
+}
+
+QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments)
+{
+    Context* c = ctx(ptr);
+    if (!c || max_segments < 1 || max_segments > qdtg::kSplitMaxSegs) return 0;
+    if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
+    c->engine->set_split_segments(max_segments);
     return 1;
 }
 

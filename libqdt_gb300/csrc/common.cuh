@@ -101,6 +101,17 @@ constexpr int kSplitMaxDepth = 9;
 constexpr int kSplitFloor = 256;
 constexpr int kSplitDefaultDepth = 7;
 constexpr int kSplitDefaultPoints = 1024;
+// segments of one split merge's seam at most (two walkers each), and the
+// node size per added segment. The block of a split merge is its walker
+// warps and an inserter warp; an SM's four sub-partitions hold 16,384
+// registers each and a block's warps are spread over them, so 7 warps of up
+// to 232 registers fit (2 a sub-partition), 9 would allow 168 at most.
+constexpr int kSplitMaxSegs = 3;
+constexpr int kSplitSegPoints = 65536;
+// deletion lists (and spare-record ranges) of one split merge: one a
+// walker, and with more than one segment one for the edges deleted before
+// the walkers start
+__host__ __device__ inline int split_lists(int segs) { return 2 * segs + (segs > 1 ? 1 : 0); }
 // bins of the records near a split merge's seam, along it (where its two
 // walkers meet)
 constexpr int kSeamBins = 64;
@@ -114,7 +125,8 @@ struct SplitPlan
     int       depth = -1;
     int       spare0 = 0;
     int       spare = 0;
-    int       per[kSplitMaxDepth + 1] = {};
+    int       per[kSplitMaxDepth + 1] = {};    // spare records (and deletion-list entries) of one walker
+    int       segs[kSplitMaxDepth + 1] = {};   // seam segments of a merge at most (2 walkers each)
     long long base[kSplitMaxDepth + 1] = {};
     int*      lists = nullptr;
 };

@@ -60,7 +60,8 @@ struct Carver
 size_t split_capacity(size_t N)
 {
     SplitPlan plan;
-    return (size_t)split_plan((int)std::min<size_t>(N, (size_t)INT32_MAX / 4), kSplitMaxDepth, kSplitFloor, plan);
+    return (size_t)split_plan((int)std::min<size_t>(N, (size_t)INT32_MAX / 4), kSplitMaxDepth, kSplitFloor,
+        kSplitMaxSegs, plan);
 }
 
 size_t carve(DeviceWork& w, char* base, size_t N)
@@ -109,6 +110,7 @@ size_t carve(DeviceWork& w, char* base, size_t N)
     b.tri_off = c.take<uint32_t>(3 * N + spare);
     b.split.lists = c.take<int>(spare);
     b.seam_hist = c.take<unsigned long long>(((size_t)2 << kSplitMaxDepth) * kSeamBins);
+    b.seam_near = c.take<unsigned long long>(((size_t)2 << kSplitMaxDepth) * kSeamBins * 2);
     b.scratch = p.scratch;
     b.tris = c.take<uint32_t>(6 * N + 3);
     b.tri_count = w.words + 1;
@@ -118,7 +120,7 @@ size_t carve(DeviceWork& w, char* base, size_t N)
 
 }  // namespace
 
-int split_plan(int m, int max_depth, int min_points, SplitPlan& plan)
+int split_plan(int m, int max_depth, int min_points, int max_segs, SplitPlan& plan)
 {
     plan.depth = -1;
     plan.spare0 = 3 * m;
@@ -134,9 +136,13 @@ int split_plan(int m, int max_depth, int min_points, SplitPlan& plan)
         // leaves room for clustered points; a walker that runs out stops or
         // frees its deleted edges first)
         const int per = (int)(3.0 * std::sqrt((double)n)) + 128;
+        // one more segment (two more walkers) per kSplitSegPoints points
+        const int segs = (int)std::max<long long>(1, std::min<long long>(std::min(max_segs, kSplitMaxSegs),
+                                                         1 + n / kSplitSegPoints));
         plan.per[d] = per;
+        plan.segs[d] = segs;
         plan.base[d] = base;
-        base += 2ll * per * (1ll << d);
+        base += (long long)split_lists(segs) * per * (1ll << d);
         plan.depth = d;
     }
     plan.spare = (int)base;
@@ -381,17 +387,21 @@ void Engine::run_graph(std::pair<uint64_t, uint64_t> key, F&& work)
         {
             if (graphs_.size() >= 32) clear_graphs();
             cudaGraph_t graph = nullptr;
+            cudaGetLastError();   // an error left by an earlier call is not this one's
             if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
             {
                 const int before = launch_counter();
                 capturing_ = true;
                 work();
                 capturing_ = false;
-                const int added = launch_counter() - before;
+                // a launch refused while recording: no graph, the launches
+                // run directly below and report it
+                const bool recorded = cudaGetLastError() == cudaSuccess;
+                const int  added = launch_counter() - before;
                 if (cudaStreamEndCapture(s, &graph) == cudaSuccess && graph)
                 {
                     cudaGraphExec_t exec = nullptr;
-                    if (cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                    if (recorded && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
                         it = graphs_.emplace(key, GraphEntry{ exec, added }).first;
                     cudaGraphDestroy(graph);
                 }
@@ -411,7 +421,9 @@ void Engine::run_graph(std::pair<uint64_t, uint64_t> key, F&& work)
             cudaGetLastError();
         }
     }
+    cudaGetLastError();
     work();
+    if (cudaGetLastError() != cudaSuccess) launch_error_ = true;
 }
 
 // Engines running a call at this moment, process-wide. The build's seam
@@ -432,6 +444,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     BuildBuffers& b = w_->build;
     HostSmall*   hs = w_->hsmall;
     info_ = RunInfo();
+    launch_error_ = false;
     info_.n = n;
     launch_counter() = 0;
     struct Busy
@@ -480,11 +493,18 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     // falling walker stops at its first, and the rising one walks alone
     {
         int* lists = b.split.lists;
-        if (split_depth_ >= 0 && b.window != 1) split_plan((int)m, split_depth_, split_min_, b.split);
+        if (split_depth_ >= 0 && b.window != 1) split_plan((int)m, split_depth_, split_min_, split_segs_, b.split);
         else b.split.depth = -1;
         b.split.lists = lists;
     }
     info_.split_depth = b.split.depth;
+    // the most seam segments of a split merge in the plan
+    auto plan_segs = [&] {
+        int sg = 0;
+        for (int d = 0; d <= b.split.depth && d <= kSplitMaxDepth; ++d) sg = std::max(sg, b.split.segs[d]);
+        return sg;
+    };
+    info_.split_segments = plan_segs();
     // the stages after the count depend only on m and the knobs: one CUDA
     // graph per such key (about 250 launches at 2.6 M points)
     auto knobs_of = [&](bool wide_kernels) {
@@ -492,7 +512,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
                ((uint64_t)b.count_filter << 17) | ((uint64_t)(timing_ ? 1 : 0) << 18) |
                ((uint64_t)(p.split_tail ? 1 : 0) << 19) | ((uint64_t)(uint32_t)b.warp_nodes << 20) |
                ((uint64_t)(b.side ? 1 : 0) << 52) | ((uint64_t)((b.split.depth + 1) & 0xF) << 53) |
-               (wide_kernels ? (1ull << 57) : 0ull);
+               (wide_kernels ? (1ull << 57) : 0ull) | ((uint64_t)(plan_segs() & 7) << 58);
     };
     if (m >= 3)
     {
@@ -526,13 +546,24 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         return cudaStreamSynchronize(s) == cudaSuccess;
     };
     if (!finish()) return S_INTERNAL;
-    if (m >= 3 && (hs->st.flags & ST_SPLIT))
-    {
-        // a split merge could not finish: the stages after the count once
-        // more, every merge with one walker
+    // a split merge that could not finish: the stages after the count once
+    // more, with one seam segment a merge when there were more (a walker
+    // above the first segment met a zero predicate), else with one walker a
+    // merge
+    auto split_retry = [&] {
         info_.split_rerun = 1;
-        b.split.depth = -1;
-        info_.split_depth = -1;
+        if (plan_segs() > 1)
+            for (int d = 0; d <= kSplitMaxDepth; ++d) b.split.segs[d] = std::min(b.split.segs[d], 1);
+        else
+        {
+            b.split.depth = -1;
+            info_.split_depth = -1;
+        }
+        info_.split_segments = plan_segs();
+    };
+    for (int tries = 0; m >= 3 && (hs->st.flags & ST_SPLIT) && b.split.depth >= 0 && tries < 2; ++tries)
+    {
+        split_retry();
         const bool w = info_.wide != 0;
         run_graph({ (uint64_t)m, knobs_of(w) }, [&] { post_sync_work(m, w); });
         if (!finish()) return S_INTERNAL;
@@ -548,12 +579,10 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         run_graph({ (uint64_t)m, knobs_of(true) }, [&] { post_sync_work(m, true); });
         if (!finish()) return S_INTERNAL;
     }
-    if (m >= 3 && (hs->st.flags & ST_SPLIT) && b.split.depth >= 0)
+    for (int tries = 0; m >= 3 && (hs->st.flags & ST_SPLIT) && b.split.depth >= 0 && tries < 2; ++tries)
     {
         // (a wide pass whose split merge failed)
-        info_.split_rerun = 1;
-        b.split.depth = -1;
-        info_.split_depth = -1;
+        split_retry();
         run_graph({ (uint64_t)m, knobs_of(true) }, [&] { post_sync_work(m, true); });
         if (!finish()) return S_INTERNAL;
     }
@@ -561,7 +590,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     info_.device_status = (int)hs->st.flags;
     take_pred_stats(info_, hs->st);
     info_.ntri = m >= 3 ? hs->words[1] : 0;
-    if (hs->st.flags & (ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX | ST_SPLIT)) return S_INTERNAL;
+    if (launch_error_ || (hs->st.flags & (ST_POOL_EMPTY | ST_GUARD | ST_BAD_INDEX | ST_SPLIT))) return S_INTERNAL;
     if (timing_)
     {
         auto el = [&](int a, int z) {

@@ -107,7 +107,8 @@ struct RunInfo
     int                    window = 0;   // warp merges' candidate window of the last call
     int                    wide = 0;     // the build ran again with the widest exact tier
     int                    split_depth = -1;   // deepest depth merged by two walkers (-1: none)
-    int                    split_rerun = 0;    // a split merge failed and the build ran again without them
+    int                    split_rerun = 0;    // a split merge failed and the build ran again (fewer segments, or without them)
+    int                    split_segments = 0; // the most seam segments of a split merge in the last pass
 };
 
 struct DeviceWork;
@@ -219,6 +220,9 @@ public:
         split_depth_ = max_depth;
         split_min_ = min_points;
     }
+    // seam segments of one split merge at most (1..kSplitMaxSegs): segments
+    // beyond the first begin at cross edges found before the merge
+    void            set_split_segments(int segs) { split_segs_ = segs; }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
@@ -258,8 +262,10 @@ private:
     bool            side_prefetch_ = true;
     int             split_depth_ = kSplitDefaultDepth;
     int             split_min_ = kSplitDefaultPoints;
+    int             split_segs_ = kSplitMaxSegs;
     size_t          limit_ = 0;   // workspace bytes cap (0: none)
     bool            capturing_ = false;   // run_graph is recording stream_
+    bool            launch_error_ = false; // a launch of this call failed (the call reports QDT_ERR_INTERNAL)
     std::map<std::pair<uint64_t, uint64_t>, GraphEntry> graphs_;   // for the current workspace
     cudaEvent_t     ev_[10] = {};
 };

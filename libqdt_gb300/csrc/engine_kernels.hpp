@@ -66,12 +66,16 @@ struct BuildBuffers
     cudaEvent_t    fork = nullptr, join = nullptr;
     SplitPlan      split;               // the top merges with two walkers (depth -1: none)
     unsigned long long* seam_hist = nullptr; // kSeamBins per node of the split depths (2^(kSplitMaxDepth+1) nodes)
+    // per node of the split depths, bin along the seam and side: the
+    // half-edge leaving the vertex nearest to the cut (distance as float
+    // bits above, half-edge below; all ones: none)
+    unsigned long long* seam_near = nullptr;
 };
 
 // The split merges of m points: depths 0.. at most max_depth whose nodes
 // hold at least min_points (>= kSplitFloor); plan.spare0 = 3 m, lists left
 // to the caller. Returns the spare records (also plan.spare).
-int split_plan(int m, int max_depth, int min_points, SplitPlan& plan);
+int split_plan(int m, int max_depth, int min_points, int max_segs, SplitPlan& plan);
 
 // Distinct points sharing x with their predecessor in (x, y) order above
 // this fraction (in 1/16) make the warp merges use a window of one

@@ -166,30 +166,58 @@ __global__ void QDTG_BUILD_BOUNDS(WARP) k_build_level(Rec* __restrict__ R, int n
     out[k] = o;
 }
 
-// The merges of one upper depth with two walkers each (seam_split.cuh): one
-// block of three warps per node, the rising walker, the falling one and the
-// ring inserter. The block's threads then remove the deleted edges
+// The merges of one upper depth with split seams (seam_split.cuh): one block
+// per node, two walker warps per seam segment (rising and falling) and the
+// ring inserter in the last warp. Before the walkers start, the first warps
+// look for the segment boundaries (one lane each) and thread 0 checks and
+// links them; a node whose boundaries cannot all be found and checked runs
+// as one segment. The block's threads then remove the deleted edges
 // together, and its first thread finds the node's extremes.
+constexpr int kSplitThreads = 32 * (kSeamWalkers + 1);
+
+// the coordinate along the seam at which the histogram's cumulative count
+// reaches the fraction f of its total, counted in the rising direction
+// (increasing y for even depths, decreasing x for odd ones); bin: its bin
+__device__ inline double seam_quantile(const unsigned long long* __restrict__ h, double2 rg, int frame, double f,
+    int& bin)
+{
+    unsigned long long total = 0;
+    for (int b = 0; b < kSeamBins; ++b) total += h[b];
+    const double       target = (frame ? 1.0 - f : f) * (double)total;
+    unsigned long long acc = 0;
+    int                b = 0;
+    while (b < kSeamBins - 1 && (double)(acc + h[b]) < target) acc += h[b++];
+    bin = b;
+    return rg.x + (b + 0.5) * ((rg.y - rg.x) / kSeamBins);
+}
+
 template <int WIN>
 __global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, const NodeOut* __restrict__ child,
     NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count, SplitPlan plan, const double* __restrict__ seam,
-    const unsigned long long* __restrict__ hist, const unsigned long long* __restrict__ box)
+    const unsigned long long* __restrict__ hist, const unsigned long long* __restrict__ near,
+    const unsigned long long* __restrict__ box)
 {
     __shared__ SeamShared S;
     __shared__ int        go;
+    __shared__ int        gl[kSeamSegs], gr[kSeamSegs];   // the boundary pairs found (half-edges, -1: none)
     const long long       k = blockIdx.x;
     const int             warp = threadIdx.x >> 5;
+    const int             lane = threadIdx.x & 31;
     int                   lo = 0, hi = 0;
     if (threadIdx.x == 0)
     {
         go = !(*(volatile unsigned*)&st->flags & kFatal) && k < (1ll << d) && node_range(m, d, k, lo, hi) &&
              hi - lo >= 4;
-        S.tail[0] = S.tail[1] = 0;
-        S.head[0] = S.head[1] = 0;
-        S.state[0] = S.state[1] = 0;
-        S.last_o = S.last_d = S.last_e = -1;
+        for (int v = 0; v < kSeamWalkers; ++v) S.tail[v] = S.head[v] = S.state[v] = S.ndel[v] = 0;
+        S.ndel[kSeamWalkers] = 0;
+        for (int j = 0; j < kSeamSegs; ++j)
+        {
+            S.last_o[j] = S.last_d[j] = S.last_e[j] = -1;
+            S.gate[j] = -1;
+            gl[j] = gr[j] = -1;
+        }
+        S.nseg = 1;
         S.first_dn = -1;
-        S.ndel[0] = S.ndel[1] = 0;
         S.base0 = S.ldo = S.rdo = S.top = -1;
         S.fhead = S.ftail = -1;
         S.fail = 0;
@@ -198,8 +226,10 @@ __global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, co
     if (!go) return;
     node_range(m, d, k, lo, hi);
     const int     n = hi - lo;
+    const int     mid = lo + n / 2;
     const NodeOut L = child[2 * k], Rn = child[2 * k + 1];
     const int     g = (d - 1) & 1;   // the parent's frame
+    const int     frame = d & 1;
     if (threadIdx.x == 0)
     {
         bool ok = !((L.fhead >= 0 && !free_tail_ok(L.ftail, lo, hi, m, nrec)) ||
@@ -233,43 +263,184 @@ __global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, co
     }
     __syncthreads();
     if (S.fail) return;
-    // the meeting point: on the node's cut (x for even d), and along the seam
-    // where half of the records near the seam lie (the histogram of the
+    // the meeting points: on the node's cut (x for even d), and along the
+    // seam at quantiles of the records near the seam (the histogram of the
     // seam prefetch), else the mean of the children's cuts
-    const double cut = seam[(1ll << d) + k];
-    double       along = 0.5 * (seam[(1ll << (d + 1)) + 2 * k] + seam[(1ll << (d + 1)) + 2 * k + 1]);
-    if (hist)
+    const double  cut = seam[(1ll << d) + k];
+    const double2 rg = seam_range(seam, box, d, k);
+    auto          at = [&](double along) { return frame ? make_double2(along, cut) : make_double2(cut, along); };
+    const unsigned long long* h = hist ? hist + ((1ll << d) + k) * kSeamBins : nullptr;
+    bool          counted = false;
+    if (h)
+        for (int b = 0; b < kSeamBins && !counted; ++b) counted = h[b] != 0;
+    const int want = (counted && near) ? plan.segs[d] : 1;
+    Builder   B{ R, nrec, st, pred_stage(st, kStageWarp, count), S.fhead, S.ftail, false };
+    // ---- segment boundaries: one lane per boundary j = 1 .. want - 1 ----
+    if (want > 1 && warp < want - 1 && lane == 0)
     {
-        const unsigned long long* h = hist + ((1ll << d) + k) * kSeamBins;
-        unsigned long long        total = 0;
-        for (int b = 0; b < kSeamBins; ++b) total += h[b];
-        if (total > 0)
+        const int j = warp + 1;
+        int       bin = 0;
+        seam_quantile(h, rg, frame, (double)j / want, bin);
+        // the vertices nearest to the cut in the nearest bins that have one
+        int hs[2] = { -1, -1 };
+        for (int side = 0; side < 2; ++side)
+            for (int t = 0; t < 2 * kSeamBins && hs[side] < 0; ++t)
+            {
+                const int b = bin + ((t & 1) ? -((t + 1) >> 1) : (t >> 1));
+                if (b < 0 || b >= kSeamBins) continue;
+                const unsigned long long key = near[(((1ll << d) + k) * kSeamBins + b) * 2 + side];
+                if (key == ~0ull) continue;
+                const int e = (int)(unsigned)key;
+                if ((unsigned)e >= 2u * (unsigned)nrec) continue;
+                const int v = R[e >> 1].org[e & 1];
+                if (side == 0 ? (v >= lo && v < mid) : (v >= mid && v < hi)) hs[side] = e;
+            }
+        if (hs[0] >= 0 && hs[1] >= 0 && seam_gabriel(R, nrec, hs[0], hs[1]))
         {
-            unsigned long long acc = 0;
-            int                b = 0;
-            while (b < kSeamBins - 1 && 2 * (acc + h[b]) < total) acc += h[b++];
-            const double2 rg = seam_range(seam, box, d, k);
-            along = rg.x + (b + 0.5) * ((rg.y - rg.x) / kSeamBins);
+            const int vl = R[hs[0] >> 1].org[hs[0] & 1], vr = R[hs[1] >> 1].org[hs[1] & 1];
+            if (vl >= lo && vl < mid && vr >= mid && vr < hi)
+            {
+                gl[j] = hs[0];
+                gr[j] = hs[1];
+            }
         }
     }
-    SeamArgs     A;
+    __syncthreads();
+    // ---- thread 0: check the boundaries and the meeting points, link them ----
+    if (threadIdx.x == 0)
+    {
+        int nseg = want;
+        for (int j = 1; j < nseg; ++j)
+            if (gl[j] < 0) nseg = 1;
+        // no two boundaries share a vertex (their ring slots are found apart)
+        for (int a = 1; a < nseg; ++a)
+            for (int c = a + 1; c < nseg; ++c)
+            {
+                const int la = R[gl[a] >> 1].org[gl[a] & 1], ra = R[gr[a] >> 1].org[gr[a] & 1];
+                const int lc = R[gl[c] >> 1].org[gl[c] & 1], rc = R[gr[c] >> 1].org[gr[c] & 1];
+                if (la == lc || ra == rc) nseg = 1;
+            }
+        double2 qs[kSeamSegs];
+        int     sl[kSeamSegs], sr[kSeamSegs];
+        if (nseg > 1)
+        {
+            // meeting points: below the first boundary and above the last at
+            // the histogram's quantiles, between two boundaries halfway
+            int bin = 0;
+            qs[0] = at(seam_quantile(h, rg, frame, 0.5 / nseg, bin));
+            qs[nseg - 1] = at(seam_quantile(h, rg, frame, (nseg - 0.5) / nseg, bin));
+            for (int j = 1; j + 1 < nseg; ++j)
+            {
+                const double2 a0 = R[gl[j] >> 1].p[gl[j] & 1], a1 = R[gr[j] >> 1].p[gr[j] & 1];
+                const double2 b0 = R[gl[j + 1] >> 1].p[gl[j + 1] & 1], b1 = R[gr[j + 1] >> 1].p[gr[j + 1] & 1];
+                const double  ca = frame ? 0.5 * (a0.x + a1.x) : 0.5 * (a0.y + a1.y);
+                const double  cb = frame ? 0.5 * (b0.x + b1.x) : 0.5 * (b0.y + b1.y);
+                qs[j] = at(0.5 * (ca + cb));
+            }
+            // each meeting point strictly above its segment's lower boundary
+            // and not above its upper one (boundary j: right end -> left end)
+            for (int j = 0; j < nseg && nseg > 1; ++j)
+            {
+                const SeamKey kq = seam_keys(qs[j], frame);
+                for (int t = j; t <= j + 1; ++t)
+                {
+                    if (t < 1 || t >= nseg) continue;
+                    const double2 po = R[gr[t] >> 1].p[gr[t] & 1], pt = R[gl[t] >> 1].p[gl[t] & 1];
+                    const bool    above =
+                        seam_q_above(qs[j], kq, po, pt, seam_keys(po, frame), seam_keys(pt, frame), B.pc);
+                    if (above != (t == j)) nseg = 1;
+                }
+            }
+        }
+        // the ring slots: right end counter-clockwise after sr, left end after sl
+        for (int j = 1; j < nseg; ++j)
+        {
+            sr[j] = seam_slot(R, nrec, gr[j], R[gl[j] >> 1].p[gl[j] & 1], B.pc);
+            sl[j] = seam_slot(R, nrec, gl[j], R[gr[j] >> 1].p[gr[j] & 1], B.pc);
+            if (sr[j] < 0 || sl[j] < 0) nseg = 1;
+        }
+        // the children's edges that cross a boundary, listed after the
+        // walkers' lists (nseg == want here: the plan's last list)
+        const int off = (int)(plan.base[d] + (long long)split_lists(plan.segs[d]) * plan.per[d] * k);
+        int       npre = 0;
+        int*      pre = plan.lists + off + 2 * want * plan.per[d];
+        for (int j = 1; j < nseg; ++j)
+            if (!seam_crossed(R, nrec, sl[j], R[gr[j] >> 1].p[gr[j] & 1], pre, npre, plan.per[d], B.pc) ||
+                !seam_crossed(R, nrec, sr[j], R[gl[j] >> 1].p[gl[j] & 1], pre, npre, plan.per[d], B.pc))
+                nseg = 1;
+        if (nseg > 1)
+        {
+            for (int i = 0; i < npre; ++i) atomicOr(reinterpret_cast<unsigned*>(&R[pre[i]].pad), kSeamPre);
+            S.ndel[2 * nseg] = npre;
+            for (int j = 1; j < nseg; ++j)
+            {
+                // the boundary edge e from r to l: the first spare record of
+                // segment j's rising walker
+                const int     kk = plan.spare0 + off + 2 * j * plan.per[d];
+                const int     e = 2 * kk;
+                const int     vr = R[gr[j] >> 1].org[gr[j] & 1], vl = R[gl[j] >> 1].org[gl[j] & 1];
+                const double2 pr = R[gr[j] >> 1].p[gr[j] & 1], pl = R[gl[j] >> 1].p[gl[j] & 1];
+                const int     yr = R[sr[j] >> 1].next[sr[j] & 1], yl = R[sl[j] >> 1].next[sl[j] & 1];
+                *reinterpret_cast<int4*>(&R[kk].org[0]) =
+                    make_int4(vr, vl, -1, (int)(seam_gate_tag(16u * (unsigned)((1ll << d) + k), j) << 16));
+                R[kk].p[0] = pr;
+                R[kk].p[1] = pl;
+                R[kk].next[0] = yr;
+                R[kk].prev[0] = sr[j];
+                R[kk].next[1] = yl;
+                R[kk].prev[1] = sl[j];
+                R[sr[j] >> 1].next[sr[j] & 1] = e;
+                R[yr >> 1].prev[yr & 1] = e;
+                R[sl[j] >> 1].next[sl[j] & 1] = e + 1;
+                R[yl >> 1].prev[yl & 1] = e + 1;
+                S.gate[j] = e;
+            }
+            for (int j = 0; j < nseg; ++j) S.q_seg[j] = qs[j];
+        }
+        else
+        {
+            // one segment: the meeting point at the median
+            double along = 0.5 * (seam[(1ll << (d + 1)) + 2 * k] + seam[(1ll << (d + 1)) + 2 * k + 1]);
+            if (counted)
+            {
+                int bin = 0;
+                along = seam_quantile(h, rg, frame, 0.5, bin);
+            }
+            S.q_seg[0] = at(along);
+        }
+        S.nseg = nseg;
+        __threadfence_block();
+    }
+    __syncthreads();
+    const int nseg = S.nseg;
+    SeamArgs  A;
     A.R = R;
     A.nrec = nrec;
-    A.tag = 4u * (unsigned)((1ll << d) + k);
-    A.q = (d & 1) ? make_double2(along, cut) : make_double2(cut, along);
-    const long long off = plan.base[d] + 2ll * plan.per[d] * k;
-    A.a0 = plan.spare0 + (int)(off + (long long)warp * plan.per[d]);
-    A.a1 = A.a0 + plan.per[d];
-    A.list[0] = plan.lists + off;
-    A.list[1] = plan.lists + off + plan.per[d];
+    A.tag = 16u * (unsigned)((1ll << d) + k);
+    const long long off = plan.base[d] + (long long)split_lists(plan.segs[d]) * plan.per[d] * k;
+    A.w = warp;
+    A.seg = warp >> 1;
+    A.nseg = nseg;
+    A.q = S.q_seg[min(A.seg, kSeamSegs - 1)];
+    A.start = -1;
+    if (warp < 2 * nseg)
+    {
+        if (warp & 1) A.start = A.seg + 1 < nseg ? S.gate[A.seg + 1] : -1;
+        else A.start = A.seg > 0 ? S.gate[A.seg] : -1;
+    }
+    A.a0 = plan.spare0 + (int)(off + (long long)warp * plan.per[d]) + ((warp & 1) == 0 && A.seg > 0 ? 1 : 0);
+    A.a1 = plan.spare0 + (int)(off + (long long)(warp + 1) * plan.per[d]);
+    A.lists = plan.lists + off;
     A.cap = plan.per[d];
     A.lim = 8 * n + 64;
-    A.frame = d & 1;
+    A.frame = frame;
     A.st = st;
-    Builder B{ R, nrec, st, pred_stage(st, kStageWarp, count), S.fhead, S.ftail, false };
-    if (warp == 0) seam_walk<false, WIN>(B, S, A, L.le, L.re, Rn.le, Rn.re);
-    else if (warp == 1) seam_walk<true, WIN>(B, S, A, L.le, L.re, Rn.le, Rn.re);
-    else if ((threadIdx.x & 31) == 0)
+    if (warp < 2 * nseg)
+    {
+        if (warp & 1) seam_walk<true, WIN>(B, S, A, L.le, L.re, Rn.le, Rn.re);
+        else seam_walk<false, WIN>(B, S, A, L.le, L.re, Rn.le, Rn.re);
+    }
+    else if (warp == kSeamWalkers && lane == 0)
     {
         bool bad = false;
         seam_inserter(S, R, nrec, A.tag, bad);
@@ -284,8 +455,8 @@ __global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, co
     {
         bool bad = false;
         int  fh = S.fhead, ft = S.ftail;
-        seam_apply(R, nrec, A.list[0], S.ndel[0], A.list[1], S.ndel[1], fh, ft, threadIdx.x, (int)blockDim.x,
-            [] { __syncthreads(); }, bad);
+        seam_apply(R, nrec, plan.lists + off, plan.per[d], S.ndel, split_lists(nseg), fh, ft, threadIdx.x,
+            (int)blockDim.x, [] { __syncthreads(); }, bad);
         if (bad) atomicOr(&st->flags, ST_SPLIT);
         if (threadIdx.x == 0)
         {
@@ -344,10 +515,14 @@ __global__ void k_seam_band(const unsigned long long* __restrict__ box, int m, d
 // seam. A merge makes about one step per point spacing along its seam, and
 // a band as wide as the local spacing holds about as many records per unit
 // of seam, in dense and sparse parts alike: the counts follow the steps, and
-// the split merge meets at their median.
+// the split merge places its segments and meeting points at their
+// quantiles. near (with hist): per node, bin and side of the cut, the
+// half-edge leaving the vertex nearest to the cut (the minimum of the
+// distance's float bits above the half-edge id: the same whatever the
+// order of the atomics), where the search for a segment boundary starts.
 __global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int d, const double* __restrict__ seam,
     uint32_t* __restrict__ list, uint32_t* __restrict__ count, uint32_t cap, unsigned long long* __restrict__ hist,
-    const unsigned long long* __restrict__ box)
+    unsigned long long* __restrict__ near, const unsigned long long* __restrict__ box)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
@@ -378,6 +553,33 @@ __global__ void k_prefetch_seams(const Rec* __restrict__ R, int nrec, int m, int
         {
             const int bin = seam_bin((d & 1) ? p0.x : p0.y, seam_range(seam, box, d, k));
             atomicAdd(&hist[((1ll << d) + k) * kSeamBins + bin], 1ull);
+        }
+        if (near)
+        {
+            // each end by its own vertex's node (a record of a split merge's
+            // spare range lies outside every node's record range)
+            for (int s = 0; s < 2; ++s)
+            {
+                const int v = s ? org.y : org.x;
+                if (v < 0 || v >= m) continue;
+                int       va = 0, vb = m;
+                long long vk = 0;
+                for (int l = 0; l < d && vb - va >= 4; ++l)
+                {
+                    const int c = va + (vb - va) / 2;
+                    if (v < c) vb = c, vk = 2 * vk;
+                    else va = c, vk = 2 * vk + 1;
+                }
+                if (vb - va < 4) continue;
+                const double2 p = s ? p1 : p0;
+                const double  sv = seam[(1ll << d) + vk];
+                const float   dv = (float)fabs(((d & 1) ? p.y : p.x) - sv);
+                const int     bin = seam_bin((d & 1) ? p.x : p.y, seam_range(seam, box, d, vk));
+                const int     side = v >= va + (vb - va) / 2 ? 1 : 0;
+                const unsigned long long key =
+                    ((unsigned long long)__float_as_uint(dv) << 32) | (unsigned)(2 * r + s);
+                atomicMin(&near[(((1ll << d) + vk) * kSeamBins + bin) * 2 + side], key);
+            }
         }
     }
 }
@@ -447,11 +649,15 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         uint32_t* const count = b.tri_count;
         cudaMemsetAsync(count, 0, sizeof(uint32_t), ps);
         unsigned long long* const hist = pd <= b.split.depth ? b.seam_hist : nullptr;
+        unsigned long long* const near = hist && b.split.segs[pd] > 1 ? b.seam_near : nullptr;
         if (hist)
             cudaMemsetAsync(hist + ((size_t)1 << pd) * kSeamBins, 0,
                 ((size_t)1 << pd) * kSeamBins * sizeof(unsigned long long), ps);
+        if (near)
+            cudaMemsetAsync(near + ((size_t)1 << pd) * kSeamBins * 2, 0xFF,
+                ((size_t)1 << pd) * kSeamBins * 2 * sizeof(unsigned long long), ps);
         k_prefetch_seams<<<(unsigned)((nrec + 255) / 256), 256, 0, ps>>>(b.recs, nrec, m, pd, b.seam, list, count,
-            (uint32_t)nrec, hist, b.box);
+            (uint32_t)nrec, hist, near, b.box);
         k_prefetch_list<<<152 * 8, 256, 0, ps>>>(b.recs, list, count, (uint32_t)nrec);
         launch_counter() += 2;
     };
@@ -485,14 +691,16 @@ void launch_build(const BuildBuffers& b, int m, cudaStream_t s)
         // at 160 points a node, 2.6 M uniform, either form takes the same)
         if (d <= b.split.depth)
         {
-            // two walkers per merge, one block per node
+            // two walkers per seam segment, one block per node
             const unsigned long long* hist = prefetch && b.seam_hist ? b.seam_hist : nullptr;
+            const unsigned long long* near = hist && b.split.segs[d] > 1 ? b.seam_near : nullptr;
             if (b.window == 1)
-                k_build_split<1><<<(unsigned)nodes, 96, 0, s>>>(b.recs, nall, b.node[(d + 1) & 1], b.node[d & 1], m,
-                    d, b.status, b.count_filter, b.split, b.seam, hist, b.box);
+                k_build_split<1><<<(unsigned)nodes, kSplitThreads, 0, s>>>(b.recs, nall, b.node[(d + 1) & 1],
+                    b.node[d & 1], m, d, b.status, b.count_filter, b.split, b.seam, hist, near, b.box);
             else
-                k_build_split<kWinDefault><<<(unsigned)nodes, 96, 0, s>>>(b.recs, nall, b.node[(d + 1) & 1],
-                    b.node[d & 1], m, d, b.status, b.count_filter, b.split, b.seam, hist, b.box);
+                k_build_split<kWinDefault><<<(unsigned)nodes, kSplitThreads, 0, s>>>(b.recs, nall,
+                    b.node[(d + 1) & 1], b.node[d & 1], m, d, b.status, b.count_filter, b.split, b.seam, hist, near,
+                    b.box);
         }
         else if ((1ll << d) <= b.warp_nodes || (m >> d) >= kWarpMinPoints)
         {

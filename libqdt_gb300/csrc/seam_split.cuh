@@ -70,8 +70,13 @@
 
 namespace qdtg {
 
-constexpr unsigned kDelRise = 0x000000FFu, kDelFall = 0x0000FF00u;
-constexpr int      kSeamQueue = 4;   // insertions a walker may have waiting
+// walkers of one merge at most: a rising and a falling one per segment of
+// the seam (walker 2 j rises in segment j, walker 2 j + 1 falls)
+constexpr int       kSeamSegs = kSplitMaxSegs;
+constexpr int       kSeamWalkers = 2 * kSeamSegs;
+constexpr unsigned  kSeamDel = 0xFFu;   // deletion flags of a record's tag word, one bit per walker
+constexpr unsigned  kSeamPre = 0x80u;   // deleted before the walkers start (crosses a segment boundary)
+constexpr int       kSeamQueue = 4;     // insertions a walker may have waiting
 constexpr long long kSeamSpin = 1ll << 24;
 
 // A ring insertion a walker asks for: the new edge e = 2 k from vo to vt
@@ -85,27 +90,34 @@ struct SeamReq
 
 struct SeamShared
 {
-    SeamReq q[2][kSeamQueue];
-    int     tail[2];               // insertions each walker posted
-    int     head[2];               // of those, the ones the inserter made
-    int     state[2];              // 1 once the walker stopped
-    int last_o, last_d, last_e;    // the falling walker's last edge (-1: none)
-    int first_dn;                  // its first edge (the upper tangent), -1: none
-    int ndel[2];                   // deletion-list fills
-    int base0, ldo, rdo, top;      // the rising walker's lower tangent, hull edges, last edge
-    int fhead, ftail;              // the node's free list
-    int fail;
+    SeamReq q[kSeamWalkers][kSeamQueue];
+    int     tail[kSeamWalkers];    // insertions each walker posted
+    int     head[kSeamWalkers];    // of those, the ones the inserter made
+    int     state[kSeamWalkers];   // 1 once the walker stopped
+    int     ndel[kSeamWalkers + 1];   // deletion-list fills; [2 nseg]: the edges deleted before the walkers
+    int     last_o[kSeamSegs], last_d[kSeamSegs], last_e[kSeamSegs];   // each falling walker's last edge (-1: none)
+    int     gate[kSeamSegs];       // the boundary edge where segment j begins (j >= 1)
+    double2 q_seg[kSeamSegs];      // each segment's meeting point
+    int     nseg;                  // segments of this merge
+    int     first_dn;              // the top falling walker's first edge (the upper tangent), -1: none
+    int     base0, ldo, rdo, top;  // the bottom rising walker's lower tangent and hull edges; the top one's last edge
+    int     fhead, ftail;          // the node's free list
+    int     fail;
 };
 
 struct SeamArgs
 {
     Rec*       R;
     int        nrec;     // pool and spare records
-    unsigned   tag;      // 4 * node tag
-    double2    q;        // the meeting point on the seam
-    int        a0, a1;   // each walker's spare records [a0, a1)
-    int*       list[2];  // deletion lists
-    int        cap;      // entries in each
+    unsigned   tag;      // 16 * node: creators tag + 1 + w; tag itself marks the segment boundaries
+    double2    q;        // the segment's meeting point on the seam
+    int        w;        // this walker
+    int        seg;      // its segment
+    int        nseg;     // segments
+    int        start;    // the boundary edge it starts from (-1: the tangent)
+    int        a0, a1;   // this walker's spare records [a0, a1)
+    int*       lists;    // deletion lists, cap entries a walker
+    int        cap;
     int        lim;      // iteration guard
     int        frame;    // the merge's frame (depth & 1): the seam runs along y (0) or -x (1)
     DevStatus* st;
@@ -131,10 +143,226 @@ __device__ __forceinline__ SeamKey seam_keys(double2 p, int frame)
     return frame ? SeamKey{ ~seam_key(p.x), seam_key(p.y) } : SeamKey{ seam_key(p.y), seam_key(p.x) };
 }
 
-// a record this walker does not see: deleted by it, or made by the other
-__device__ __forceinline__ bool seam_skip(unsigned pad, unsigned mydel, unsigned other)
+// Creators in a record's tag word (bits 16..31), per merge (tag = 16 *
+// node): tag + 1 + w for walker w's edges (w < 8), tag + 9 + j for the
+// boundary edge where segment j begins (j >= 1, seen by the two walkers that
+// start there).
+__device__ __forceinline__ unsigned seam_gate_tag(unsigned tag, int j) { return tag + 9u + (unsigned)j; }
+
+// a record walker w does not see: deleted by it (mydel: its flag, and
+// kSeamPre for a walker that starts at a segment boundary), or made in the
+// same merge by another walker, or a segment boundary other than the one it
+// starts at
+__device__ __forceinline__ bool seam_skip(unsigned pad, unsigned mydel, unsigned tag, unsigned mytag, unsigned mygate)
 {
-    return (pad & mydel) != 0u || (pad >> 16) == other;
+    const unsigned c = pad >> 16;
+    return (pad & mydel) != 0u || ((c & ~15u) == tag && c != mytag && c != mygate);
+}
+
+// q strictly above the cross edge po -> pt (po on the right, pt on the left
+// side) in the rising direction of the seam: the seam keys decide when both
+// endpoints lie on one side of q along the seam, else one exact orientation.
+__device__ __forceinline__ bool seam_q_above(double2 q, SeamKey kq, double2 po, double2 pt, SeamKey ko, SeamKey kt,
+    PredCounters* pc)
+{
+    if (!(ko.across == kq.across && kt.across == kq.across))
+    {
+        if (ko.up < kq.up && kt.up < kq.up) return true;
+        if (ko.up > kq.up && kt.up > kq.up) return false;
+    }
+    const double2 dqo = make_double2(sub_rn(po.x, q.x), sub_rn(po.y, q.y));
+    const double2 dqt = make_double2(sub_rn(pt.x, q.x), sub_rn(pt.y, q.y));
+    int sg = orient2d_f32(dqt.x, dqt.y, dqo.x, dqo.y);
+    if (!sg) sg = orient2d_slow(pt.x, pt.y, po.x, po.y, q.x, q.y, pc);
+    return sg > 0;
+}
+
+// ---- segment boundaries ----
+//
+// A seam is cut into segments at cross edges that are known to be edges of
+// the merged triangulation before any walker runs: pairs (l, r), l a vertex
+// of the left child and r of the right one, such that l is the unique
+// left vertex nearest to r and r the unique right vertex nearest to l. A
+// point p of the left side inside or on the circle with diameter lr would
+// be nearer to r than l (the angle lpr is at least a right angle), and a
+// point of the right side nearer to l than r: that circle holds no other
+// point, so lr is an edge of every Delaunay triangulation of the merged
+// points, the reference's included, and the sequential merge passes it.
+//
+// When the sequential merge makes lr its base edge, no edge of either child
+// crosses lr any more (a new cross edge never crosses a remaining edge: the
+// ones it would cross are the candidates its step deletes). The children's
+// edges that cross lr are deleted before the walkers start (kSeamPre); from
+// then on each walker keeps that invariant itself, so a walker that starts
+// at lr sees, above (or, falling, below) it, the map the sequential merge
+// sees there, up to edges at l and r that its own first steps delete.
+
+// sign of |p - t|^2 - |s - t|^2, 0 when the double evaluation cannot tell.
+// Each difference carries a relative error of at most u = 2^-53, each
+// square and sum one more rounding: the computed value is within 5 u (A +
+// B) of the exact one (A, B the two squared lengths); 8 u is the bound.
+__device__ __forceinline__ int seam_farther(double2 p, double2 s, double2 t)
+{
+    const double ax = __dsub_rn(p.x, t.x), ay = __dsub_rn(p.y, t.y);
+    const double bx = __dsub_rn(s.x, t.x), by = __dsub_rn(s.y, t.y);
+    const double a = __dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay));
+    const double b = __dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by));
+    const double sum = a + b;
+    if (!(sum > 1e-280) || !(sum < 1e280)) return 0;
+    const double v = __dsub_rn(a, b);
+    const double bound = 8.0 * 1.1102230246251565e-16 * sum;
+    return v > bound ? 1 : (v < -bound ? -1 : 0);
+}
+
+// The vertex of one child nearest to t, by steepest descent along the
+// child's edges from the origin of half-edge e (before the merge a ring
+// holds only the child's own edges; in a Delaunay triangulation a vertex
+// that is not the nearest has a strictly nearer neighbour). Returns a
+// half-edge leaving that vertex, every neighbour of which is strictly
+// farther from t; -1 when a comparison is too close to call, an index is
+// out of range or the walk runs long.
+static __device__ int seam_nearest(const Rec* __restrict__ R, int nrec, int e, double2 t, int steps)
+{
+    const unsigned lim2 = 2u * (unsigned)nrec;
+    if ((unsigned)e >= lim2) return -1;
+    for (int step = 0; step < steps; ++step)
+    {
+        const double2 pv = R[e >> 1].p[e & 1];
+        int           best = -1;
+        double2       pb = pv;
+        int           x = e;
+        for (int deg = 0;; ++deg)
+        {
+            if (deg > 64) return -1;
+            const double2 pu = R[x >> 1].p[(x & 1) ^ 1];
+            const int     c = seam_farther(pu, pv, t);
+            if (c == 0) return -1;
+            if (c < 0 && (best < 0 || seam_farther(pu, pb, t) < 0))
+            {
+                best = x;
+                pb = pu;
+            }
+            x = R[x >> 1].next[x & 1];
+            if ((unsigned)x >= lim2) return -1;
+            if (x == e) break;
+        }
+        if (best < 0) return e;
+        e = best ^ 1;   // leaves the nearer neighbour
+    }
+    return -1;
+}
+
+// A segment boundary near the start half-edges hl (leaving a vertex of the
+// left child) and hr (of the right one): alternating nearest-vertex walks
+// until the pair settles. On success hl and hr leave l and r.
+static __device__ bool seam_gabriel(const Rec* __restrict__ R, int nrec, int& hl, int& hr)
+{
+    int l = hl, r = hr;
+    for (int it = 0; it < 12; ++it)
+    {
+        l = seam_nearest(R, nrec, l, R[r >> 1].p[r & 1], 512);
+        if (l < 0) return false;
+        const int r2 = seam_nearest(R, nrec, r, R[l >> 1].p[l & 1], 512);
+        if (r2 < 0) return false;
+        if (R[r2 >> 1].org[r2 & 1] == R[r >> 1].org[r & 1])
+        {
+            hl = l;
+            hr = r2;
+            return true;
+        }
+        r = r2;
+    }
+    return false;
+}
+
+// lnext(e): the next edge of e's left face
+__device__ __forceinline__ int seam_lnext(const Rec* __restrict__ R, int e)
+{
+    return R[(e ^ 1) >> 1].prev[(e ^ 1) & 1];
+}
+
+// The records of one child's edges that the segment from v (the origin of
+// slot, whose counter-clockwise wedge up to next(slot) holds the direction
+// to t, seam_slot) towards t crosses, in order, appended to out[cnt ..) and
+// not already tagged kSeamPre (an edge two boundaries cross is listed
+// once). The walk goes from face to face of the child's triangulation until
+// it leaves the child's hull. False when a vertex lies on the segment's
+// line, a face is not a triangle where one must be, an index is out of
+// range or more than cap edges are listed.
+static __device__ bool seam_crossed(const Rec* __restrict__ R, int nrec, int slot, double2 t, int* out, int& cnt,
+    int cap, PredCounters* pc)
+{
+    const unsigned lim2 = 2u * (unsigned)nrec;
+    auto           ok = [&](int e) { return (unsigned)e < lim2; };
+    auto           dst = [&](int e) { return R[e >> 1].p[(e & 1) ^ 1]; };
+    if (!ok(slot)) return false;
+    const double2 v = R[slot >> 1].p[slot & 1];
+    const int     y = R[slot >> 1].next[slot & 1];
+    if (!ok(y)) return false;
+    if (y == slot) return true;   // a single edge: the segment leaves at once
+    const double2 pa0 = dst(slot), pb0 = dst(y);
+    if (orient2d_sign(v.x, v.y, pa0.x, pa0.y, pb0.x, pb0.y, pc) <= 0) return true;   // the outer wedge
+    // the left face of slot is the triangle (v, a, b); the segment leaves it
+    // through f = a -> b
+    int f = seam_lnext(R, slot);
+    if (!ok(f) || !ok(seam_lnext(R, f)) || seam_lnext(R, seam_lnext(R, f)) != slot) return false;
+    for (int it = 0; it < 256; ++it)
+    {
+        const int k = f >> 1;
+        if (!((unsigned)R[k].pad & kSeamPre))
+        {
+            bool seen = false;
+            for (int i = 0; i < cnt && !seen; ++i) seen = out[i] == k;
+            if (!seen)
+            {
+                if (cnt >= cap) return false;
+                out[cnt++] = k;
+            }
+        }
+        // the face across f: (b, a, c)
+        const int g = f ^ 1, h1 = seam_lnext(R, g);
+        if (!ok(h1)) return false;
+        const int h2 = seam_lnext(R, h1);
+        if (!ok(h2)) return false;
+        if (seam_lnext(R, h2) != g) return true;   // the outer face: the segment left the hull
+        const double2 pb = R[g >> 1].p[g & 1], pa = R[g >> 1].p[(g & 1) ^ 1], pc2 = dst(h1);
+        // (a hull of three edges is a 3-cycle too, turning clockwise)
+        if (orient2d_sign(pb.x, pb.y, pa.x, pa.y, pc2.x, pc2.y, pc) <= 0) return true;
+        const int     sa = orient2d_sign(v.x, v.y, t.x, t.y, pa.x, pa.y, pc);
+        const int     sc = orient2d_sign(v.x, v.y, t.x, t.y, pc2.x, pc2.y, pc);
+        if (sa == 0 || sc == 0) return false;
+        f = sc == sa ? h2 : h1;   // c on a's side: out through c -> b, else through a -> c
+    }
+    return false;
+}
+
+// The ring slot of a new edge from the origin v of half-edge a towards t:
+// the half-edge x of v's ring such that the direction to t lies strictly
+// inside the counter-clockwise wedge from x to next(x). -1 when an
+// orientation with an edge of the ring is zero or the ring runs long.
+static __device__ int seam_slot(const Rec* __restrict__ R, int nrec, int a, double2 t, PredCounters* pc)
+{
+    const unsigned lim2 = 2u * (unsigned)nrec;
+    if ((unsigned)a >= lim2) return -1;
+    const double2 v = R[a >> 1].p[a & 1];
+    int           x = a;
+    for (int deg = 0; deg <= 64; ++deg)
+    {
+        const int y = R[x >> 1].next[x & 1];
+        if ((unsigned)y >= lim2) return -1;
+        const double2 px = R[x >> 1].p[(x & 1) ^ 1], py = R[y >> 1].p[(y & 1) ^ 1];
+        const int     sxt = orient2d_sign(v.x, v.y, px.x, px.y, t.x, t.y, pc);
+        if (sxt == 0) return -1;
+        if (y == x) return x;   // one edge: every other direction
+        const int sty = orient2d_sign(v.x, v.y, t.x, t.y, py.x, py.y, pc);
+        if (sty == 0) return -1;
+        const int  sxy = orient2d_sign(v.x, v.y, px.x, px.y, py.x, py.y, pc);
+        const bool inside = sxy > 0 ? (sxt > 0 && sty > 0) : (sxt > 0 || sty > 0);
+        if (inside) return x;
+        x = y;
+        if (x == a) return -1;
+    }
+    return -1;
 }
 
 // one window entry: half-edge e, its successor along the side's direction,
@@ -183,19 +411,20 @@ __device__ __forceinline__ int& link_w(Rec* R, int e, bool fwd, int w)
     return (fwd != (w != 0)) ? R[e >> 1].next[e & 1] : R[e >> 1].prev[e & 1];
 }
 
-// The inserter (one thread of the block's third warp): makes every ring
-// insertion of both walkers, each walker's in its order, reading the
+// The inserter (one thread of the block's last warp): makes every ring
+// insertion of every walker, each walker's in its order, reading the
 // anchors' neighbours as the rings are then; being the only thread that
 // writes ring links while the walkers run, it needs no lock. It returns
-// once both walkers stopped and their requests are done.
+// once every walker stopped and their requests are done.
 static __device__ void seam_inserter(SeamShared& S, Rec* R, int nrec, unsigned tag, bool& bad)
 {
     const unsigned lim2 = 2u * (unsigned)nrec;
+    const int      nw = 2 * S.nseg;
     long long      idle = 0;
     while (!bad)
     {
         bool did = false;
-        for (int w = 0; w < 2; ++w)
+        for (int w = 0; w < nw; ++w)
         {
             const int h = S.head[w];
             if (h >= *(volatile int*)&S.tail[w]) continue;
@@ -204,12 +433,13 @@ static __device__ void seam_inserter(SeamShared& S, Rec* R, int nrec, unsigned t
             const int     k = r.k, vo = r.vo, vt = r.vt, Q1 = r.Q1, P2 = r.P2;
             const double2 po = make_double2(r.po.x, r.po.y), pt = make_double2(r.pt.x, r.pt.y);
             const int     e = 2 * k;
+            const int     m = w & 1;   // the falling walkers' rotation is the mirror
             if ((unsigned)k >= (unsigned)nrec || (unsigned)Q1 >= lim2 || (unsigned)P2 >= lim2)
             {
                 bad = true;
                 break;
             }
-            const int P1 = link_w(R, Q1, false, w), Q2 = link_w(R, P2, true, w);
+            const int P1 = link_w(R, Q1, false, m), Q2 = link_w(R, P2, true, m);
             if ((unsigned)P1 >= lim2 || (unsigned)Q2 >= lim2)
             {
                 bad = true;
@@ -218,15 +448,15 @@ static __device__ void seam_inserter(SeamShared& S, Rec* R, int nrec, unsigned t
             *reinterpret_cast<int4*>(&R[k].org[0]) = make_int4(vo, vt, -1, (int)((tag + 1u + (unsigned)w) << 16));
             R[k].p[0] = po;
             R[k].p[1] = pt;
-            link_w(R, e, true, w) = Q1;
-            link_w(R, e, false, w) = P1;
-            link_w(R, e + 1, true, w) = Q2;
-            link_w(R, e + 1, false, w) = P2;
+            link_w(R, e, true, m) = Q1;
+            link_w(R, e, false, m) = P1;
+            link_w(R, e + 1, true, m) = Q2;
+            link_w(R, e + 1, false, m) = P2;
             __threadfence_block();   // the new edge's own links before the links to it
-            link_w(R, P1, true, w) = e;
-            link_w(R, Q1, false, w) = e;
-            link_w(R, P2, true, w) = e + 1;
-            link_w(R, Q2, false, w) = e + 1;
+            link_w(R, P1, true, m) = e;
+            link_w(R, Q1, false, m) = e;
+            link_w(R, P2, true, m) = e + 1;
+            link_w(R, Q2, false, m) = e + 1;
             __threadfence_block();   // the links before the count that covers them
             *(volatile int*)&S.head[w] = h + 1;
             did = true;
@@ -237,29 +467,44 @@ static __device__ void seam_inserter(SeamShared& S, Rec* R, int nrec, unsigned t
             continue;
         }
         if (*(volatile int*)&S.fail) return;
-        if (*(volatile int*)&S.state[0] && *(volatile int*)&S.state[1] &&
-            S.head[0] == *(volatile int*)&S.tail[0] && S.head[1] == *(volatile int*)&S.tail[1])
-            return;
+        bool all = true;
+        for (int w = 0; w < nw && all; ++w)
+            all = *(volatile int*)&S.state[w] && S.head[w] == *(volatile int*)&S.tail[w];
+        if (all) return;
         if (++idle > kSeamSpin) bad = true;
         __nanosleep(20);
     }
 }
 
-// The physical deletion of the tagged edges in lists[0][0, n0) and
-// lists[1][0, n1), by nt threads (tid), then their records onto the free
-// list (fhead, ftail), first list in order, then the second without the
-// records the first holds. SYNC: barrier of the nt threads.
+// The physical deletion of the tagged edges in the nl deletion lists (list
+// v: lists + v * cap, n[v] entries; the walkers' lists, then with more than
+// two lists the edges deleted before the walkers), by nt threads (tid), then
+// their records onto the free list (fhead, ftail), the lists in order, each
+// walker's without the records an earlier walker's list or the last list
+// holds (an edge two walkers deleted). SYNC: barrier of the nt threads.
 template <class SyncF>
-__device__ void seam_apply(Rec* R, int nrec, const int* l0, int n0, int* l1, int n1, int& fhead, int& ftail, int tid,
-    int nt, SyncF sync, bool& bad)
+__device__ void seam_apply(Rec* R, int nrec, int* lists, int cap, const int* n, int nl, int& fhead, int& ftail,
+    int tid, int nt, SyncF sync, bool& bad)
 {
-    auto dead = [&](int e) { return ((unsigned)R[e >> 1].pad & (kDelRise | kDelFall)) != 0u; };
+    auto dead = [&](int e) { return ((unsigned)R[e >> 1].pad & kSeamDel) != 0u; };
+    int total = 0;
+    for (int v = 0; v < nl; ++v) total += n[v];
+    // entry i of the concatenated lists
+    auto at_ref = [&](int i) -> int& {
+        int v = 0;
+        while (v + 1 < nl && i >= n[v]) i -= n[v++];
+        return lists[(size_t)v * cap + i];
+    };
+    auto list_of = [&](int i) {
+        int v = 0;
+        while (v + 1 < nl && i >= n[v]) i -= n[v++];
+        return v;
+    };
     // rings: the first half-edge of every run of deleted ones links its
     // predecessor to the run's successor
-    for (int i = tid; i < 2 * (n0 + n1); i += nt)
+    for (int i = tid; i < 2 * total; i += nt)
     {
-        const int idx = i >> 1;
-        const int k = idx < n0 ? l0[idx] : l1[idx - n0];
+        const int k = at_ref(i >> 1);
         if ((unsigned)k >= (unsigned)nrec)
         {
             bad = true;
@@ -284,29 +529,31 @@ __device__ void seam_apply(Rec* R, int nrec, const int* l0, int n0, int* l1, int
         R[q >> 1].prev[q & 1] = p;
     }
     sync();
-    // the second list without the records of the first
-    for (int i = tid; i < n1; i += nt)
+    // each list without the records of the lists before it
+    for (int i = tid; i < total; i += nt)
     {
-        const int k = l1[i];
-        if ((unsigned)k >= (unsigned)nrec || ((unsigned)R[k].pad & kDelRise)) l1[i] = -1;
+        int&      k = at_ref(i);
+        const int v = list_of(i);
+        const bool walker = nl <= 2 || v + 1 < nl;
+        if (walker && (v > 0 || nl > 2) &&
+            ((unsigned)k >= (unsigned)nrec || ((unsigned)R[k].pad & (((1u << v) - 1u) | (nl > 2 ? kSeamPre : 0u)))))
+            k = -1;
     }
     sync();
-    // the free list: the first list, the second, then the old list
+    // the free list: the lists in order, then the old list
     const int old = fhead;
-    const int total = n0 + n1;
-    auto at = [&](int i) { return i < n0 ? l0[i] : l1[i - n0]; };
     if (!bad)
         for (int i = tid; i < total; i += nt)
         {
-            const int k = at(i);
+            const int k = at_ref(i);
             if (k < 0) continue;
             int j = i + 1;
-            while (j < total && at(j) < 0) ++j;
-            *reinterpret_cast<int4*>(&R[k].org[0]) = make_int4(-1, -1, j < total ? at(j) : old, 0);
+            while (j < total && at_ref(j) < 0) ++j;
+            *reinterpret_cast<int4*>(&R[k].org[0]) = make_int4(-1, -1, j < total ? at_ref(j) : old, 0);
         }
     int first = -1, last = -1;
-    for (int i = 0; i < total && first < 0; ++i) first = at(i);
-    for (int i = total - 1; i >= 0 && last < 0; --i) last = at(i);
+    for (int i = 0; i < total && first < 0; ++i) first = at_ref(i);
+    for (int i = total - 1; i >= 0 && last < 0; --i) last = at_ref(i);
     if (first >= 0)
     {
         if (old < 0) ftail = last;
@@ -315,9 +562,14 @@ __device__ void seam_apply(Rec* R, int nrec, const int* l0, int n0, int* l1, int
     sync();
 }
 
-// One walker of a split merge: MIRROR false, the rising walker (warp 0),
-// true the falling one (warp 1). The rising walker takes B's free list
-// first; B.fhead/ftail come back through S.
+// One walker of a split merge: MIRROR false, the rising walker of its
+// segment (walker 2 j), true the falling one (walker 2 j + 1). The bottom
+// rising walker (walker 0) takes B's free list first; B.fhead/ftail come
+// back through S. The bottom rising walker is the reference's merge from
+// the lower tangent; every other walker starts at a segment boundary (or
+// the upper tangent) and stops at the first predicate that is zero: the
+// falling ones hand the rest of their segment to its rising walker, a
+// rising one above the bottom fails the merge (ST_SPLIT).
 template <bool MIRROR, int WIN>
 __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo, int ldi, int rdi, int rdo)
 {
@@ -333,10 +585,17 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     const int      ca = qd >> 2, rb = qd & 3;
     const bool     combo = j >= 4 && j < 12 && ca < WIN && rb < WIN;
     const int      jj = slot ? j : 0;
-    const int      w = MIRROR ? 1 : 0, o = 1 - w;
-    const unsigned mydel = MIRROR ? kDelFall : kDelRise;
-    const unsigned mytag = A.tag + (MIRROR ? 2u : 1u), other = A.tag + (MIRROR ? 1u : 2u);
-    int* const     list = A.list[w];
+    const int      w = A.w, o = w ^ 1;   // o: the other walker of the segment
+    const unsigned mydel = 1u << w;
+    // the edges deleted before the walkers: gone for the walkers that start
+    // at a segment boundary; the bottom rising and the top falling walker
+    // see the children as the sequential merges do
+    const unsigned myskip = mydel | (A.start >= 0 ? kSeamPre : 0u);
+    const unsigned mytag = A.tag + 1u + (unsigned)w;
+    const unsigned mygate = seam_gate_tag(A.tag, (w + 1) >> 1);   // the boundary it starts or ends at
+    const bool     strict = MIRROR || A.seg > 0;   // stops at the first zero
+    const bool     top_seg = A.seg == A.nseg - 1;
+    int* const     list = A.lists + (size_t)w * A.cap;
     int            fill = 0;
     bool           bad = false;
     int            a_next = A.a0;
@@ -387,7 +646,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             if ((unsigned)x >= 2u * (unsigned)nrec) break;
             x = link_of<MIRROR>(R, x, fwd);
             if ((unsigned)x >= 2u * (unsigned)nrec) break;
-            if (x == e || !seam_skip((unsigned)R[x >> 1].pad, mydel, other)) return x;
+            if (x == e || !seam_skip((unsigned)R[x >> 1].pad, myskip, A.tag, mytag, mygate)) return x;
         }
         bad = true;
         return e;
@@ -396,7 +655,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     auto vorg = [&](int e) { return R[min((unsigned)(e >> 1), (unsigned)(nrec - 1))].org[e & 1]; };
     // a record for a new edge: the free list (rising walker), then the spare range
     auto alloc = [&]() -> int {
-        if (!MIRROR && B.fhead >= 0 && B.fhead < nrec)
+        if (w == 0 && B.fhead >= 0 && B.fhead < nrec)
         {
             const int k = B.fhead;
             B.fhead = flink;
@@ -407,9 +666,9 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     };
     // after an allocation: the next head's link, needed only at the next one
     auto refill_link = [&]() {
-        if (!MIRROR) flink = (B.fhead >= 0 && B.fhead < nrec) ? R[B.fhead].link : -1;
+        if (w == 0) flink = (B.fhead >= 0 && B.fhead < nrec) ? R[B.fhead].link : -1;
     };
-    auto have_record = [&]() { return (!MIRROR && B.fhead >= 0) || a_next < A.a1; };
+    auto have_record = [&]() { return (w == 0 && B.fhead >= 0) || a_next < A.a1; };
     // a ring insertion for the inserter (lane 0): e = 2 k from vo to vt right
     // before Q1 in this walker's rotation, sym(e) right after P2. Every lane
     // keeps the anchors of the requests not yet made: a window that reaches
@@ -468,16 +727,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     // orientation.
     const SeamKey kq = seam_keys(A.q, A.frame);
     auto q_above = [&](double2 po, double2 pt, SeamKey ko, SeamKey kt) {
-        if (!(ko.across == kq.across && kt.across == kq.across))
-        {
-            if (ko.up < kq.up && kt.up < kq.up) return true;
-            if (ko.up > kq.up && kt.up > kq.up) return false;
-        }
-        const double2 dqo = make_double2(sub_rn(po.x, A.q.x), sub_rn(po.y, A.q.y));
-        const double2 dqt = make_double2(sub_rn(pt.x, A.q.x), sub_rn(pt.y, A.q.y));
-        int sg = orient2d_f32(dqt.x, dqt.y, dqo.x, dqo.y);
-        if (!sg) sg = orient2d_slow(pt.x, pt.y, po.x, po.y, A.q.x, A.q.y, B.pc);
-        return sg > 0;
+        return seam_q_above(A.q, kq, po, pt, ko, kt, B.pc);
     };
 
     // ---- the tangent and the first edge (lane 0) ----
@@ -486,11 +736,19 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     double2 tp_o = make_double2(0, 0), tp_d = tp_o;
     SeamKey k_o = {}, k_d = {};   // the base edge's vertices' seam keys (lane 0)
     bool stop = false;   // the falling walker has nothing (more) to do
+    const bool from_gate = A.start >= 0;   // starts at a segment boundary
+    int        gate_o = -1, gate_d = -1;       // the boundary above this rising walker's segment
+    if (lane == 0 && !MIRROR && !top_seg)
+    {
+        const int g = S.gate[A.seg + 1];
+        gate_o = vorg(g);
+        gate_d = vorg(sym(g));
+    }
     if (lane == 0)
     {
         refill_link();
         int l = ldi, r = rdi;
-        if (MIRROR)
+        if (MIRROR && !from_gate)
         {
             // the upper tangent starts from the hull edges above the lower
             // ones at the inner extremes (builder.hxx:253-261 mirrored)
@@ -504,7 +762,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                        B.pc) <= 0;
         }
         // leftOf(org(r), l) ? l = lnext(l) : rightOf(org(l), r) ? r = rprev(r)
-        for (int it = 0; !stop && !bad; ++it)
+        for (int it = 0; !from_gate && !stop && !bad; ++it)
         {
             if (it > 2 * A.lim)
             {
@@ -538,9 +796,9 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
         }
         if (!bad && !stop)
         {
-            // the tangent edge org(r) -> org(l)
-            const int     vo = vorg(r), vt = vorg(l);
-            const double2 po = porg(r), pt = porg(l);
+            // the tangent edge org(r) -> org(l), or the boundary edge
+            const int     vo = from_gate ? vorg(A.start) : vorg(r), vt = from_gate ? vorg(sym(A.start)) : vorg(l);
+            const double2 po = from_gate ? porg(A.start) : porg(r), pt = from_gate ? porg(sym(A.start)) : porg(l);
             t_o = vo, t_d = vt, tp_o = po, tp_d = pt;
             k_o = seam_keys(po, A.frame);
             k_d = seam_keys(pt, A.frame);
@@ -555,12 +813,20 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             if (!MIRROR && !bad && *(volatile int*)&S.state[o])
             {
                 __threadfence_block();
-                if (S.last_e >= 0 && S.last_o == vo && S.last_d == vt) taken = S.last_e;
+                const int j = A.seg;
+                if (S.last_e[j] >= 0 && S.last_o[j] == vo && S.last_d[j] == vt) taken = S.last_e[j];
             }
             if (!bad && !stop)
             {
                 if (taken >= 0)
                     basel = taken;
+                else if (from_gate)
+                {
+                    // the windows start at the boundary edge's raw neighbours
+                    basel = A.start;
+                    Bb = link_of<MIRROR>(R, basel, false);
+                    Fsb = link_of<MIRROR>(R, sym(basel), true);
+                }
                 else
                 {
                     const int k = alloc();
@@ -583,7 +849,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                         tp2 = l;
                     }
                 }
-                if (!MIRROR && !bad)
+                if (!MIRROR && !bad && !from_gate)
                 {
                     S.base0 = basel;
                     if (vorg(l) == vorg(ldo)) ldo = sym(basel);
@@ -591,7 +857,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                     S.ldo = ldo;
                     S.rdo = rdo;
                 }
-                if (MIRROR && !bad) S.first_dn = basel;
+                if (MIRROR && !bad && !from_gate) S.first_dn = basel;
                 if (!MIRROR && taken >= 0) stop = true;   // the falling walker made the whole chain
             }
         }
@@ -653,21 +919,35 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                     stop = true;
                     break;
                 }
+                if (w != 0)
+                {
+                    // a rising walker above the bottom one has nobody to hand
+                    // its segment to
+                    bad = true;
+                    dbg_why = 10;
+                    break;
+                }
 #if QDTG_SPLIT_DEBUG
                 ++dbg_flush;
 #endif
-                // the rising walker frees every deleted edge, once the falling one
-                // stopped and every insertion is made
+                // the bottom rising walker frees every deleted edge, once every
+                // other walker stopped and every insertion is made
                 bool ok = true;
                 if (lane == 0)
                 {
-                    ok = wait_other() && wait_queue(kSeamQueue);
-                    for (long long i = 0; ok && i < kSeamSpin; ++i)
-                    {
-                        if (*(volatile int*)&S.head[o] == *(volatile int*)&S.tail[o]) break;
-                        if (i + 1 == kSeamSpin) ok = false;
-                        __nanosleep(20);
-                    }
+                    ok = wait_queue(kSeamQueue);
+                    for (int v = 1; ok && v < 2 * A.nseg; ++v)
+                        for (long long i = 0;; ++i)
+                        {
+                            if (*(volatile int*)&S.state[v] && *(volatile int*)&S.head[v] == *(volatile int*)&S.tail[v])
+                                break;
+                            if (i + 1 >= kSeamSpin || *(volatile int*)&S.fail)
+                            {
+                                ok = false;
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
                 }
                 ok = __shfl_sync(FULL, (int)ok, 0) != 0;
                 if (!ok)
@@ -678,8 +958,11 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 __threadfence_block();
                 int  fh2 = __shfl_sync(FULL, B.fhead, 0), ft2 = __shfl_sync(FULL, B.ftail, 0);
                 bool b2 = false;
-                seam_apply(R, nrec, list, fill, A.list[1], *(volatile int*)&S.ndel[1], fh2, ft2, lane, 32,
-                    [] { __syncwarp(); }, b2);
+                int  nd[kSeamWalkers + 1];
+#pragma unroll
+                for (int v = 0; v <= kSeamWalkers; ++v) nd[v] = v == 0 ? fill : *(volatile int*)&S.ndel[v];
+                seam_apply(R, nrec, A.lists, A.cap, nd, split_lists(A.nseg), fh2, ft2, lane, 32, [] { __syncwarp(); },
+                    b2);
                 fh2 = __shfl_sync(FULL, fh2, 0);
                 ft2 = __shfl_sync(FULL, ft2, 0);
                 if (__any_sync(FULL, b2))
@@ -691,7 +974,8 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 B.ftail = ft2;
                 if (lane == 0) refill_link();
                 fill = 0;
-                if (lane == 0) S.ndel[1] = 0;
+                if (lane == 0)
+                    for (int v = 1; v < split_lists(A.nseg); ++v) S.ndel[v] = 0;
                 // the raw ring links held lose the records just freed
                 int f = 0, b = 0;
                 if (lane == 0)
@@ -733,7 +1017,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                         break;
                     }
                     const SEnt x = load_sent<MIRROR>(R, cur, nrec, !left);
-                    skipped = skipped || seam_skip(x.pad, mydel, other);
+                    skipped = skipped || seam_skip(x.pad, myskip, A.tag, mytag, mygate);
                     if (i == jj) mine = x;
                     if (i == jj + 1) succ = x;
                     cur = x.nx;
@@ -746,7 +1030,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 {
                     if ((unsigned)cur >= 2u * (unsigned)nrec) break;
                     const SEnt x = load_sent<MIRROR>(R, cur, nrec, !left);
-                    if (!seam_skip(x.pad, mydel, other))
+                    if (!seam_skip(x.pad, myskip, A.tag, mytag, mygate))
                     {
                         if (found == jj) mine = x;
                         if (found == jj + 1) succ = x;
@@ -824,7 +1108,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             const int      dr = runr ? (zr ? __ffs(zr) - 1 : WIN) : 0;
             const int      srcL = min(dl, WIN - 1), srcR = 16 + min(dr, WIN - 1);
             const bool     overL = dl == WIN, overR = dr == WIN;
-            if (MIRROR)
+            if (strict)
             {
                 // the zeros the sequential merge would have evaluated
                 unsigned used = 0;
@@ -860,7 +1144,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             const bool del = slot && j < (left ? dl : dr);
             if (del)
             {
-                reinterpret_cast<volatile unsigned char*>(&R[mine.e >> 1].pad)[w] = 1;
+                atomicOr(reinterpret_cast<unsigned*>(&R[mine.e >> 1].pad), mydel);
                 list[fill + (left ? j : dl + j)] = mine.e >> 1;
             }
             fill += dl + dr;
@@ -894,19 +1178,25 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
 #if QDTG_SPLIT_DEBUG
         const long long dbg_m0 = clock64();
 #endif
+        if (tie && !MIRROR)
+        {
+            bad = true;   // a zero for a rising walker above the bottom one
+            dbg_why = 9;
+        }
         if (bad || stop || tie) break;
         if (!lv && !rv)
         {
             // the end of the chain: for the falling walker, the whole chain
-            // lies at or above q; the rising walker must have met the falling one
+            // lies at or above q; the rising walker must have met the falling
+            // one (and only the top segment's reaches the end)
             if (!MIRROR)
             {
-                bool b2 = false;
-                if (lane == 0)
+                bool b2 = !top_seg;
+                if (lane == 0 && !b2)
                 {
                     if (!*(volatile int*)&S.state[o] && !wait_other()) b2 = true;
                     __threadfence_block();
-                    if (*(volatile int*)&S.last_e >= 0)
+                    if (*(volatile int*)&S.last_e[A.seg] >= 0)
                     {
                         b2 = true;
                         dbg_why = 7;
@@ -936,7 +1226,15 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 if (!bad && *(volatile int*)&S.state[o])
                 {
                     __threadfence_block();
-                    if (S.last_e >= 0 && S.last_o == vo && S.last_d == vt) taken = S.last_e;
+                    const int j = A.seg;
+                    if (S.last_e[j] >= 0 && S.last_o[j] == vo && S.last_d[j] == vt) taken = S.last_e[j];
+                }
+                // a rising walker never reaches the boundary above its segment
+                // without taking its falling walker's last edge
+                if (!bad && taken < 0 && !top_seg && vo == gate_o && vt == gate_d)
+                {
+                    bad = true;
+                    dbg_why = 11;
                 }
             }
         }
@@ -1006,15 +1304,15 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     {
         const int why = __shfl_sync(FULL, dbg_why, 0) | __reduce_or_sync(FULL, (unsigned)dbg_why);
         if (lane == 0 && bad)
-            printf("split FAIL node=%u w=%d why=%d steps=%d posted=%d head=%d\n", A.tag / 4u, w, why, dbg_steps, posted,
+            printf("split FAIL node=%u w=%d why=%d steps=%d posted=%d head=%d\n", A.tag / 16u, w, why, dbg_steps, posted,
                 *(volatile int*)&S.head[w]);
     }
 #endif
 #if QDTG_SPLIT_DEBUG
-    if (lane == 0 && A.tag / 4u < 16u)
+    if (lane == 0 && A.tag / 16u < 16u)
         printf("split node=%u w=%d steps=%d passes=%d del=%d flush=%d stop=%d bad=%d chain=%d cyc=%lld wait=%lld "
                "lock=%lld win=%lld pred=%lld conn=%lld snap=%lld mid=%lld post=%lld spare=%d\n",
-            A.tag / 4u, w, dbg_steps, dbg_passes, dbg_del, dbg_flush, (int)stop, (int)bad, (int)done_chain,
+            A.tag / 16u, w, dbg_steps, dbg_passes, dbg_del, dbg_flush, (int)stop, (int)bad, (int)done_chain,
             clock64() - dbg_t0, dbg_wait, dbg_lock, dbg_win, dbg_pred, dbg_conn, dbg_snap, dbg_mid, dbg_post,
             a_next - A.a0);
 #endif
@@ -1026,16 +1324,19 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
         {
             if (basel >= 0 && !bad)
             {
-                S.last_e = basel;
-                S.last_o = bo;
-                S.last_d = bd;
+                S.last_e[A.seg] = basel;
+                S.last_o[A.seg] = bo;
+                S.last_d[A.seg] = bd;
             }
         }
         else
         {
-            S.top = basel;
-            S.fhead = B.fhead;
-            S.ftail = B.ftail;
+            if (top_seg) S.top = basel;
+            if (w == 0)
+            {
+                S.fhead = B.fhead;
+                S.ftail = B.ftail;
+            }
         }
         __threadfence_block();
         *(volatile int*)&S.state[w] = 1;

@@ -235,7 +235,8 @@ def test_split_merges_same_result(lib):
     fallback would hide a wrong walk); two runs give identical arrays; the
     1M uniform workload keeps the reference's digest. The merge window is
     fixed at 2, so that lattice-like input (where a call leaves the split
-    merges off by default) runs them too."""
+    merges off by default) runs them too. One seam segment a merge here;
+    test_split_segments_same_result covers more."""
     spec = next(s for s in _DIGESTS if s["name"] == "uniform_1m")
     inputs = [("uniform_1m", C.make_large(spec))] + list(_split_inputs())
     for name, p in inputs:
@@ -243,6 +244,7 @@ def test_split_merges_same_result(lib):
         for split in (True, False, True):
             with G.Triangulation(lib) as t:
                 assert t.set_merge_window(2)
+                assert t.set_split_segments(1)
                 if not split:
                     assert t.set_split_merges(-1)
                 assert t.execute(p) == 0, name
@@ -260,6 +262,58 @@ def test_split_merges_same_result(lib):
         assert np.array_equal(r1, r0), name
         if name == "uniform_1m":
             assert _digest(O.canonical(t1).astype(np.int64)) == spec["serial"]["tri_digest"]
+
+
+# inputs in general position: their split merges must run with more than one
+# seam segment and without falling back
+_GENERAL = ("uniform_1m", "uniform_2p6m", "gauss", "skewed", "blobs", "line")
+
+
+def test_split_segments_same_result(lib):
+    """Seams cut into segments at boundary edges (mutually nearest vertices
+    of the two halves, the children's edges that cross them deleted first),
+    two walkers a segment: for 1, 2 and 3 segments the canonical triangles
+    and representatives of the one-walker build, on every kind of input, and
+    identical arrays on a second run. On input in general position the
+    merges use the segments without falling back; on degenerate input a
+    merge whose walker above the first segment meets a zero runs again with
+    one segment (the same result)."""
+    spec = next(s for s in _DIGESTS if s["name"] == "uniform_1m")
+    inputs = [("uniform_1m", C.make_large(spec)), ("uniform_2p6m", W.uniform(2600000, 7))] + list(_split_inputs())
+    for name, p in inputs:
+        with G.Triangulation(lib) as t:
+            assert t.set_merge_window(2)
+            assert t.set_split_merges(-1)
+            assert t.execute(p) == 0, name
+            want_t = O.canonical(t.triangles_array())
+            want_r = t.rep_array().copy()
+        for segs in (1, 2, 3):
+            runs = []
+            for _ in range(2):
+                with G.Triangulation(lib) as t:
+                    assert t.set_merge_window(2)
+                    assert t.set_split_segments(segs)
+                    assert t.execute(p) == 0, (name, segs)
+                    info = t.run_info()
+                    runs.append((t.triangles_array().copy(), t.rep_array().copy(), info))
+            (t1, r1, i1), (t2, r2, _) = runs
+            assert np.array_equal(t1, t2) and np.array_equal(r1, r2), (name, segs)
+            assert np.array_equal(O.canonical(t1), want_t), (name, segs)
+            assert np.array_equal(r1, want_r), (name, segs)
+            assert i1["split_segments"] <= segs, (name, segs)
+            if name in _GENERAL:
+                assert i1["split_rerun"] == 0, (name, segs)
+                assert i1["split_segments"] == segs, (name, segs)
+        if name == "uniform_1m":
+            assert _digest(O.canonical(t1).astype(np.int64)) == spec["serial"]["tri_digest"]
+
+
+def test_split_segments_knob(lib):
+    with G.Triangulation(lib) as t:
+        assert not t.set_split_segments(0)
+        assert not t.set_split_segments(4)
+        for segs in (1, 2, 3):
+            assert t.set_split_segments(segs)
 
 
 def test_split_merges_off_on_lattice_like_input(lib):
