@@ -94,16 +94,17 @@ QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
    GPU. No counterpart in the reference, whose merges are sequential. */
 QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
 
-/* Seam segments of one split merge at most (1..4, default 4; a node gets
+/* Seam segments of one split merge at most (1..3, default 3; a node gets
    one more segment per 65,536 points, on calls of at least 65,536 points).
    Segments beyond the first begin at cross edges found before the merge:
    pairs of mutually nearest vertices of the two halves, which are edges of
    every Delaunay triangulation of the merged points; each segment is walked
    by a rising and a falling walker. The triangulation is the same for
-   every value (a merge whose walkers above the first segment meet a
-   cocircular or collinear configuration runs again with one walker).
-   Returns 1, or 0 for a NULL context, a value out of range or no usable
-   GPU. No counterpart in the reference. */
+   every value: a call whose walkers above the first segment meet a
+   cocircular or collinear configuration runs its build again with one
+   segment a merge (qdtg_run_info.split_rerun). Returns 1, or 0 for a NULL
+   context, a value out of range or no usable GPU. No counterpart in the
+   reference, whose merges are sequential. */
 QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments);
 
 /* Caps the device bytes of the context's workspace (0: no cap, the

@@ -1,61 +1,76 @@
-// Split merges: the seam of one top-level merge walked by two warps at once.
+// Split merges: the seam of one top-level merge walked by several warps at
+// once.
 //
 // The merge of the reference builder (builder.hxx:251-285) is one chain of
 // bubble steps from the lower common tangent up to the upper one. At the top
 // of the tree that chain is long (about 3,600 steps at the root of 2.6 M
-// uniform points) and nothing else runs beside it. Here a rising walker runs
-// the reference's merge from the lower tangent (warp 0 of the block) while a
-// falling walker (warp 1) runs its mirror image (the same merge with the
-// rotations and the predicate signs reversed) down from the upper tangent.
-// Both are warp merges with the candidate window of warp_merge.
+// uniform points) and nothing else runs beside it. Here the seam is cut into
+// up to kSeamSegs segments, each walked by two warps: a rising walker runs
+// the reference's merge up from the segment's lower end while a falling
+// walker runs its mirror image (the same merge with the rotations and the
+// predicate signs reversed) down from its upper end. All are warp merges
+// with the candidate window of warp_merge.
+//
+// Segment ends. The first segment starts at the lower tangent and the last
+// ends at the upper one; the others meet at boundary edges found before the
+// walkers start: pairs of mutually nearest vertices of the two halves, which
+// are edges of every Delaunay triangulation of the merged points (see the
+// segment boundaries below), linked into the rings first, with the
+// children's edges that cross them deleted.
 //
 // The walkers never see each other's work:
-// * each record carries a tag word (Rec::pad): one byte per walker marks the
-//   edges it deleted, and bits 16..31 name the walker that made the edge;
-// * deletions only set the walker's byte: the edge stays in its rings until
+// * each record carries a tag word (Rec::pad): one bit per walker marks the
+//   edges it deleted (kSeamPre the ones deleted before the walkers), and
+//   bits 16..31 name the walker that made the edge, or the boundary;
+// * deletions only set the walker's bit: the edge stays in its rings until
 //   the merge ends, and the walker that deleted it steps over it;
-// * insertions are real ring insertions, but the other walker steps over
+// * insertions are real ring insertions, but the other walkers step over
 //   them; each one goes right next to one of the new edge's anchors (the
 //   walker's own previous edge or the candidate edge it chose), never next
-//   to an edge of the other walker, so the two walkers' insertions keep
-//   their order in every ring they share.
+//   to an edge of another walker, so the walkers' insertions keep their
+//   order in every ring they share.
 // So each walker sees exactly the map its own sequential merge would have
-// at that step: the rising walker makes the reference's decisions, and the
-// falling walker those of the mirror merge.
+// at that step: the bottom rising walker makes the reference's decisions,
+// and every other walker those of a sequential merge (or its mirror)
+// started at its segment's end.
 //
-// Where they meet: q is a point on the seam (the node's cut coordinate,
-// and the mean of its children's cuts along the seam). The rising walker
-// keeps the edges that have q strictly above them, the falling walker the
-// others; the test is one exact orientation, the same in both walkers. The
-// rising walker's first edge without q above is the falling walker's last
-// one: it stops there and takes that edge. The mirror merge decides like
-// the reference only where no predicate it evaluates is zero, so the
-// falling walker stops at its first zero (cocircular or collinear points),
-// and then the rising walker goes on past q up to the falling walker's last
-// edge. (Without zeros every decision holds for all small perturbations of
-// the points; the edges made and deleted are then those of every Delaunay
-// triangulation of the points, the reference's included.) A rising walker
-// whose chain does not meet that edge reports ST_SPLIT and the call runs
-// again without split merges.
+// Where two walkers of a segment meet: q is a point on the seam (on the
+// node's cut line, at a quantile of the records near the seam, or halfway
+// between two boundaries). The rising walker keeps the edges that have q
+// strictly above them, the falling walker the others; the test is one exact
+// orientation, the same in both walkers. The rising walker's first edge
+// without q above is the falling walker's last one: it stops there and
+// takes that edge. A merge started anywhere but at the lower tangent
+// decides like the reference only where no predicate it evaluates is zero
+// (without zeros every decision holds for all small perturbations of the
+// points; the edges made and deleted are then those of every Delaunay
+// triangulation of the points, the reference's included). So a falling
+// walker stops at its first zero (cocircular or collinear points), and the
+// rising walker of its segment goes on past q up to the falling walker's
+// last edge; a rising walker above the first segment that meets a zero
+// fails the merge. A failed split merge (that, or a rising walker whose
+// chain does not meet its falling walker's last edge) reports ST_SPLIT and
+// the call runs again with one segment a merge, and then, if that fails
+// too, without split merges.
 //
 // Spare records: a walker makes its edges before the deleted ones are
 // freed, so each one has a range of spare records after the pool (the
-// rising one takes its node's free list first). When the falling walker's
-// range or deletion list runs out it stops; when the rising walker's runs
-// out, it waits for the falling walker to stop and then frees every deleted
-// edge (seam_apply) before it goes on.
+// bottom rising one takes its node's free list first). When a falling
+// walker's range or deletion list runs out it stops; when the bottom rising
+// walker's runs out, it waits for every other walker to stop and then frees
+// every deleted edge (seam_apply) before it goes on; another rising walker
+// fails the merge.
 //
 // At the end the block removes the deleted edges from their rings and puts
-// their records on the node's free list, the rising walker's in its order,
-// then the falling walker's: the record ids, and so the output, do not
-// depend on how the two warps were scheduled.
+// their records on the node's free list, the walkers' lists in order, then
+// the edges deleted before the walkers: the record ids, and so the output,
+// do not depend on how the warps were scheduled.
 //
-// Shared rings: a walker inserts under a block-wide lock, and keeps in
-// shared memory the two origins of its last kSeamLog insertions. The ring
-// neighbours a walker inserts next to were read earlier; they are read again
-// only when the other walker has inserted at the same vertex since.
+// Shared rings: one thread of the block (the inserter) makes every ring
+// insertion, each walker's in its order, reading the anchors' neighbours
+// as the rings are then.
 //
-// Every wait on the other warp is bounded; a wait that runs out, like any
+// Every wait on another warp is bounded; a wait that runs out, like any
 // other failure of a split merge, reports ST_SPLIT and ends the merge.
 #pragma once
 
