@@ -95,7 +95,8 @@ QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
 QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
 
 /* Seam segments of one split merge at most (1..3, default 3; a node gets
-   one more segment per 65,536 points, on calls of at least 65,536 points).
+   one more segment per segment_points points, at least 1,024, default
+   16,384; on calls of at least 65,536 points).
    Segments beyond the first begin at cross edges found before the merge:
    pairs of mutually nearest vertices of the two halves, which are edges of
    every Delaunay triangulation of the merged points; each segment is walked
@@ -105,7 +106,7 @@ QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
    segment a merge (qdtg_run_info.split_rerun). Returns 1, or 0 for a NULL
    context, a value out of range or no usable GPU. No counterpart in the
    reference, whose merges are sequential. */
-QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments);
+QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments, int segment_points);
 
 /* Caps the device bytes of the context's workspace (0: no cap, the
    default). A batch call whose workspace would exceed the cap returns

@@ -119,7 +119,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.qdtg_set_side_prefetch.restype = ctypes.c_int
     lib.qdtg_set_split_merges.argtypes = [P, ctypes.c_int, ctypes.c_int]
     lib.qdtg_set_split_merges.restype = ctypes.c_int
-    lib.qdtg_set_split_segments.argtypes = [P, ctypes.c_int]
+    lib.qdtg_set_split_segments.argtypes = [P, ctypes.c_int, ctypes.c_int]
     lib.qdtg_set_split_segments.restype = ctypes.c_int
     lib.qdtg_set_workspace_limit.argtypes = [P, ctypes.c_size_t]
     lib.qdtg_set_workspace_limit.restype = ctypes.c_int
@@ -270,10 +270,11 @@ class Triangulation(qdt_api.Context):
         min_points points); max_depth -1: one walker per merge."""
         return self.lib.qdtg_set_split_merges(self.ptr, int(max_depth), int(min_points)) == 1
 
-    def set_split_segments(self, max_segments: int) -> bool:
-        """Seam segments of one split merge at most (1..4): segments beyond
-        the first begin at cross edges found before the merge."""
-        return self.lib.qdtg_set_split_segments(self.ptr, int(max_segments)) == 1
+    def set_split_segments(self, max_segments: int, segment_points: int = 16384) -> bool:
+        """Seam segments of one split merge at most (1..3), one more per
+        segment_points points of the node: segments beyond the first begin
+        at cross edges found before the merge."""
+        return self.lib.qdtg_set_split_segments(self.ptr, int(max_segments), int(segment_points)) == 1
 
     def filter_stats(self) -> dict:
         """Per-stage predicate statistics of the last batch call (counted

@@ -612,12 +612,13 @@ QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points)
     return 1;
 }
 
-QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments)
+QDT_API int qdtg_set_split_segments(qdt_t* ptr, int max_segments, int segment_points)
 {
     Context* c = ctx(ptr);
-    if (!c || max_segments < 1 || max_segments > qdtg::kSplitMaxSegs) return 0;
+    if (!c || max_segments < 1 || max_segments > qdtg::kSplitMaxSegs || segment_points < qdtg::kSplitSegFloor)
+        return 0;
     if (qdtg::ensure_engine(*c) != QDT_OK) return 0;
-    c->engine->set_split_segments(max_segments);
+    c->engine->set_split_segments(max_segments, segment_points);
     return 1;
 }
 

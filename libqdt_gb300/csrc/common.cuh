@@ -102,12 +102,13 @@ constexpr int kSplitFloor = 256;
 constexpr int kSplitDefaultDepth = 7;
 constexpr int kSplitDefaultPoints = 1024;
 // segments of one split merge's seam at most (two walkers each), and the
-// node size per added segment. The block of a split merge is its walker
+// default node size per added segment (floor kSplitSegFloor). The block of a split merge is its walker
 // warps and an inserter warp; an SM's four sub-partitions hold 16,384
 // registers each and a block's warps are spread over them, so 7 warps of up
 // to 232 registers fit (2 a sub-partition), 9 would allow 168 at most.
 constexpr int kSplitMaxSegs = 3;
-constexpr int kSplitSegPoints = 65536;
+constexpr int kSplitSegPoints = 16384;
+constexpr int kSplitSegFloor = 1024;
 // deletion lists (and spare-record ranges) of one split merge: one a
 // walker, and with more than one segment one for the edges deleted before
 // the walkers start

@@ -61,7 +61,7 @@ size_t split_capacity(size_t N)
 {
     SplitPlan plan;
     return (size_t)split_plan((int)std::min<size_t>(N, (size_t)INT32_MAX / 4), kSplitMaxDepth, kSplitFloor,
-        kSplitMaxSegs, plan);
+        kSplitMaxSegs, kSplitSegFloor, plan);
 }
 
 size_t carve(DeviceWork& w, char* base, size_t N)
@@ -120,7 +120,7 @@ size_t carve(DeviceWork& w, char* base, size_t N)
 
 }  // namespace
 
-int split_plan(int m, int max_depth, int min_points, int max_segs, SplitPlan& plan)
+int split_plan(int m, int max_depth, int min_points, int max_segs, int seg_points, SplitPlan& plan)
 {
     plan.depth = -1;
     plan.spare0 = 3 * m;
@@ -136,9 +136,9 @@ int split_plan(int m, int max_depth, int min_points, int max_segs, SplitPlan& pl
         // leaves room for clustered points; a walker that runs out stops or
         // frees its deleted edges first)
         const int per = (int)(3.0 * std::sqrt((double)n)) + 128;
-        // one more segment (two more walkers) per kSplitSegPoints points
+        // one more segment (two more walkers) per seg_points points
         const int segs = (int)std::max<long long>(1, std::min<long long>(std::min(max_segs, kSplitMaxSegs),
-                                                         1 + n / kSplitSegPoints));
+                                                         1 + n / std::max(seg_points, kSplitSegFloor)));
         plan.per[d] = per;
         plan.segs[d] = segs;
         plan.base[d] = base;
@@ -493,7 +493,8 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     // falling walker stops at its first, and the rising one walks alone
     {
         int* lists = b.split.lists;
-        if (split_depth_ >= 0 && b.window != 1) split_plan((int)m, split_depth_, split_min_, split_segs_, b.split);
+        if (split_depth_ >= 0 && b.window != 1)
+            split_plan((int)m, split_depth_, split_min_, split_segs_, split_seg_points_, b.split);
         else b.split.depth = -1;
         b.split.lists = lists;
     }
@@ -505,6 +506,14 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         return sg;
     };
     info_.split_segments = plan_segs();
+    // the graph key's first word: m, and above it the plan's segments a
+    // depth (2 bits each)
+    auto key_of_m = [&] {
+        uint64_t k = (uint64_t)m;
+        for (int d = 0; d <= b.split.depth && d <= kSplitMaxDepth; ++d)
+            k |= (uint64_t)(b.split.segs[d] & 3) << (32 + 2 * d);
+        return k;
+    };
     // the stages after the count depend only on m and the knobs: one CUDA
     // graph per such key (about 250 launches at 2.6 M points)
     auto knobs_of = [&](bool wide_kernels) {
@@ -519,7 +528,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         // a counting call runs the kernels that count every predicate call
         // (the wide ones) from the start
         const bool counting = b.count_filter != 0;
-        run_graph({ (uint64_t)m, knobs_of(counting) }, [&] { post_sync_work(m, counting); });
+        run_graph({ key_of_m(), knobs_of(counting) }, [&] { post_sync_work(m, counting); });
         info_.wide = counting ? 1 : 0;
     }
     else
@@ -565,7 +574,7 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     {
         split_retry();
         const bool w = info_.wide != 0;
-        run_graph({ (uint64_t)m, knobs_of(w) }, [&] { post_sync_work(m, w); });
+        run_graph({ key_of_m(), knobs_of(w) }, [&] { post_sync_work(m, w); });
         if (!finish()) return S_INTERNAL;
     }
     bool wide = false;
@@ -576,14 +585,14 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
         // kernels leave out: the stages after the count once more with the
         // kernels that have it
         info_.wide = 1;
-        run_graph({ (uint64_t)m, knobs_of(true) }, [&] { post_sync_work(m, true); });
+        run_graph({ key_of_m(), knobs_of(true) }, [&] { post_sync_work(m, true); });
         if (!finish()) return S_INTERNAL;
     }
     for (int tries = 0; m >= 3 && (hs->st.flags & ST_SPLIT) && b.split.depth >= 0 && tries < 2; ++tries)
     {
         // (a wide pass whose split merge failed)
         split_retry();
-        run_graph({ (uint64_t)m, knobs_of(true) }, [&] { post_sync_work(m, true); });
+        run_graph({ key_of_m(), knobs_of(true) }, [&] { post_sync_work(m, true); });
         if (!finish()) return S_INTERNAL;
     }
     info_.launches = launch_counter();

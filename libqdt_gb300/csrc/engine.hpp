@@ -220,9 +220,14 @@ public:
         split_depth_ = max_depth;
         split_min_ = min_points;
     }
-    // seam segments of one split merge at most (1..kSplitMaxSegs): segments
-    // beyond the first begin at cross edges found before the merge
-    void            set_split_segments(int segs) { split_segs_ = segs; }
+    // seam segments of one split merge at most (1..kSplitMaxSegs), one more
+    // per seg_points points of the node: segments beyond the first begin at
+    // cross edges found before the merge
+    void            set_split_segments(int segs, int seg_points)
+    {
+        split_segs_ = segs;
+        split_seg_points_ = seg_points;
+    }
     int             warp_nodes() const { return warp_nodes_; }
 
 private:
@@ -263,6 +268,7 @@ private:
     int             split_depth_ = kSplitDefaultDepth;
     int             split_min_ = kSplitDefaultPoints;
     int             split_segs_ = kSplitMaxSegs;
+    int             split_seg_points_ = kSplitSegPoints;
     size_t          limit_ = 0;   // workspace bytes cap (0: none)
     bool            capturing_ = false;   // run_graph is recording stream_
     bool            launch_error_ = false; // a launch of this call failed (the call reports QDT_ERR_INTERNAL)

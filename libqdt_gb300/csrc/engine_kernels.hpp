@@ -75,7 +75,7 @@ struct BuildBuffers
 // The split merges of m points: depths 0.. at most max_depth whose nodes
 // hold at least min_points (>= kSplitFloor); plan.spare0 = 3 m, lists left
 // to the caller. Returns the spare records (also plan.spare).
-int split_plan(int m, int max_depth, int min_points, int max_segs, SplitPlan& plan);
+int split_plan(int m, int max_depth, int min_points, int max_segs, int seg_points, SplitPlan& plan);
 
 // Distinct points sharing x with their predecessor in (x, y) order above
 // this fraction (in 1/16) make the warp merges use a window of one
