@@ -32,6 +32,7 @@ struct DeviceWork
     void*        block = nullptr;
     size_t       bytes = 0;
     size_t       cap = 0;      // capacity in points
+    size_t       spare_cap = 0;   // spare records of the split merges
     PrepBuffers  prep;
     BuildBuffers build;
     double2*     pts = nullptr;
@@ -55,13 +56,18 @@ struct Carver
     }
 };
 
-// spare records (and deletion-list entries) of the split merges of N points
-// at every depth they may run at
+// spare records (and deletion-list entries) of the split merges of N
+// points: the default plan (seam segments included), and one segment a
+// merge at every depth and node size the knobs allow. A call whose plan
+// needs more (segments on deeper depths or smaller nodes) runs its merges
+// with one segment.
 size_t split_capacity(size_t N)
 {
-    SplitPlan plan;
-    return (size_t)split_plan((int)std::min<size_t>(N, (size_t)INT32_MAX / 4), kSplitMaxDepth, kSplitFloor,
-        kSplitMaxSegs, kSplitSegFloor, plan);
+    SplitPlan  plan;
+    const int  n = (int)std::min<size_t>(N, (size_t)INT32_MAX / 4);
+    const auto a = (size_t)split_plan(n, kSplitDefaultDepth, kSplitDefaultPoints, kSplitMaxSegs, kSplitSegPoints, plan);
+    const auto b = (size_t)split_plan(n, kSplitMaxDepth, kSplitFloor, 1, kSplitSegFloor, plan);
+    return std::max(a, b);
 }
 
 size_t carve(DeviceWork& w, char* base, size_t N)
@@ -103,6 +109,7 @@ size_t carve(DeviceWork& w, char* base, size_t N)
     w.words = c.take<uint32_t>(8);
     p.status_u32 = w.words;
     const size_t spare = split_capacity(N);
+    w.spare_cap = spare;
     b.recs = c.take<Rec>(3 * N + spare);
     b.V = p.V;
     b.vid = p.vid;
@@ -132,13 +139,17 @@ int split_plan(int m, int max_depth, int min_points, int max_segs, int seg_point
         // the largest node of depth d
         const long long n = ((long long)m + (1ll << d) - 1) >> d;
         if (n < min_points) break;
-        // each walker: about half the seam's cross edges (3 per sqrt(n)
-        // leaves room for clustered points; a walker that runs out stops or
-        // frees its deleted edges first)
-        const int per = (int)(3.0 * std::sqrt((double)n)) + 128;
         // one more segment (two more walkers) per seg_points points
         const int segs = (int)std::max<long long>(1, std::min<long long>(std::min(max_segs, kSplitMaxSegs),
                                                          1 + n / std::max(seg_points, kSplitSegFloor)));
+        // each walker's records and deletion-list entries: about half the
+        // seam's cross edges (3 sqrt(n) leaves room for clustered points; a
+        // walker that runs out stops or frees its deleted edges first), and
+        // with several segments twice that: a rising walker above the first
+        // segment cannot free records while the others run, and a long seam
+        // (heavy-tailed points: 4 times 3 sqrt(n)) would otherwise stop both
+        // walkers of a segment
+        const int per = ((int)(3.0 * std::sqrt((double)n)) + 128) * (segs > 1 ? 2 : 1);
         plan.per[d] = per;
         plan.segs[d] = segs;
         plan.base[d] = base;
@@ -494,7 +505,13 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     {
         int* lists = b.split.lists;
         if (split_depth_ >= 0 && b.window != 1)
+        {
             split_plan((int)m, split_depth_, split_min_, split_segs_, split_seg_points_, b.split);
+            // a plan beyond the workspace's spare records: one segment a merge
+            if ((size_t)b.split.spare > w_->spare_cap)
+                split_plan((int)m, split_depth_, split_min_, 1, split_seg_points_, b.split);
+            if ((size_t)b.split.spare > w_->spare_cap) b.split.depth = -1;
+        }
         else b.split.depth = -1;
         b.split.lists = lists;
     }

@@ -213,6 +213,8 @@ __global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, co
         for (int j = 0; j < kSeamSegs; ++j)
         {
             S.last_o[j] = S.last_d[j] = S.last_e[j] = -1;
+            S.rstop[j] = S.fdone[j] = S.fpub[j] = S.rdone[j] = 0;
+            S.rlast_o[j] = S.rlast_d[j] = S.rlast_e[j] = -1;
             S.gate[j] = -1;
             gl[j] = gr[j] = -1;
         }
@@ -357,7 +359,26 @@ __global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, co
         {
             sr[j] = seam_slot(R, nrec, gr[j], R[gl[j] >> 1].p[gl[j] & 1], B.pc);
             sl[j] = seam_slot(R, nrec, gl[j], R[gr[j] >> 1].p[gr[j] & 1], B.pc);
-            if (sr[j] < 0 || sl[j] < 0) nseg = 1;
+            if (sr[j] < 0 || sl[j] < 0)
+            {
+                nseg = 1;
+                break;
+            }
+            // the first candidates of the rising walker that starts here (the
+            // next left edge counter-clockwise after the boundary, the next
+            // right edge clockwise): a zero among their first tests (points
+            // cocircular or collinear with the boundary) would fail that
+            // walker, so such a boundary is not used
+            const double2 pl = R[gl[j] >> 1].p[gl[j] & 1], pr = R[gr[j] >> 1].p[gr[j] & 1];
+            const int     ya = R[sl[j] >> 1].next[sl[j] & 1];
+            const double2 pa = R[ya >> 1].p[(ya & 1) ^ 1], pb = R[sr[j] >> 1].p[(sr[j] & 1) ^ 1];
+            if (orient2d_sign(pa.x, pa.y, pl.x, pl.y, pr.x, pr.y, B.pc) == 0 ||
+                orient2d_sign(pb.x, pb.y, pl.x, pl.y, pr.x, pr.y, B.pc) == 0 ||
+                incircle_sign(pl.x, pl.y, pr.x, pr.y, pa.x, pa.y, pb.x, pb.y, B.pc) == 0)
+            {
+                nseg = 1;
+                break;
+            }
         }
         // the children's edges that cross a boundary, listed after the
         // walkers' lists (nseg == want here: the plan's last list)

@@ -111,6 +111,16 @@ struct SeamShared
     int     state[kSeamWalkers];   // 1 once the walker stopped
     int     ndel[kSeamWalkers + 1];   // deletion-list fills; [2 nseg]: the edges deleted before the walkers
     int     last_o[kSeamSegs], last_d[kSeamSegs], last_e[kSeamSegs];   // each falling walker's last edge (-1: none)
+    // a rising walker above the first segment that ran out of records stops
+    // early (rstop) at its last edge (rlast_*), and its falling walker goes
+    // on down to that edge; fdone: the falling walker finished (set before
+    // it reads rstop, as rstop is set before the rising walker reads fdone)
+    int     rstop[kSeamSegs], fdone[kSeamSegs];
+    // above the first segment a falling walker that reaches q publishes its
+    // last edge (fpub) and waits until its rising walker is done (rdone) or
+    // stopped early
+    int     fpub[kSeamSegs], rdone[kSeamSegs];
+    int     rlast_o[kSeamSegs], rlast_d[kSeamSegs], rlast_e[kSeamSegs];
     int     gate[kSeamSegs];       // the boundary edge where segment j begins (j >= 1)
     double2 q_seg[kSeamSegs];      // each segment's meeting point
     int     nseg;                  // segments of this merge
@@ -635,13 +645,15 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
         return MIRROR ? -s : s;
     };
     // the other warp has stopped (bounded wait)
+    // the segment's falling walker has stopped or published its last edge
+    auto other_done = [&]() { return *(volatile int*)&S.state[o] || *(volatile int*)&S.fpub[A.seg]; };
     auto wait_other = [&]() -> bool {
 #if QDTG_SPLIT_DEBUG
         const long long c0 = clock64();
 #endif
         for (long long i = 0; i < kSeamSpin; ++i)
         {
-            if (*(volatile int*)&S.state[o])
+            if (other_done())
             {
 #if QDTG_SPLIT_DEBUG
                 dbg_wait += clock64() - c0;
@@ -745,6 +757,17 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
         return seam_q_above(A.q, kq, po, pt, ko, kt, B.pc);
     };
 
+    // (falling) going on past q down to the last edge of a rising walker that
+    // stopped early; lane 0: the walker finished its part, did the rising one
+    // stop early?
+    bool down_more = false;
+    auto fall_done_lane0 = [&]() -> bool {
+        const int j = A.seg;
+        *(volatile int*)&S.fdone[j] = 1;
+        __threadfence_block();
+        return *(volatile int*)&S.rstop[j] != 0;
+    };
+
     // ---- the tangent and the first edge (lane 0) ----
     int     basel = -1, Fsb = 0, Bb = 0, tq1 = -1, tp2 = -1;
     int     t_o = 0, t_d = 0;                      // the first edge's endpoints (lane 0)
@@ -821,11 +844,11 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             int           taken = -1;
             if (MIRROR)
                 stop = above;
-            else if (!above && !*(volatile int*)&S.state[o])
+            else if (!above && !other_done())
             {
                 if (!wait_other()) bad = true;
             }
-            if (!MIRROR && !bad && *(volatile int*)&S.state[o])
+            if (!MIRROR && !bad && other_done())
             {
                 __threadfence_block();
                 const int j = A.seg;
@@ -936,10 +959,28 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 }
                 if (w != 0)
                 {
-                    // a rising walker above the bottom one has nobody to hand
-                    // its segment to
-                    bad = true;
-                    dbg_why = 10;
+                    // a rising walker above the bottom one stops at its last
+                    // edge and hands the rest of its segment to the falling
+                    // walker, unless that one has finished
+                    bool fail = false;
+                    if (lane == 0)
+                    {
+                        const int j = A.seg;
+                        S.rlast_e[j] = basel;
+                        S.rlast_o[j] = bo;
+                        S.rlast_d[j] = bd;
+                        __threadfence_block();
+                        *(volatile int*)&S.rstop[j] = 1;
+                        __threadfence_block();
+                        fail = *(volatile int*)&S.fdone[j] != 0;
+                    }
+                    if (__shfl_sync(FULL, (int)fail, 0))
+                    {
+                        bad = true;
+                        dbg_why = 10;
+                    }
+                    else
+                        stop = true;
                     break;
                 }
 #if QDTG_SPLIT_DEBUG
@@ -1097,7 +1138,9 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             int        so = 0;
             if (slot && !wrap) so = orient(mine.p, pbd, pbo);
             const bool valid = so > 0;
-            const bool vtie = slot && (wrap || so == 0);
+            // (for a rising walker a wrap is the reference's own "not valid";
+            // only a zero orientation is a tie)
+            const bool vtie = slot && ((MIRROR && wrap) || (!wrap && so == 0));
             const int  ia = slot ? bd : ad, ib = slot ? bo : bd, ic = slot ? mine.d : bo, id = slot ? succ.d : bdst;
             const double2 qa = slot ? pbd : pa, qb = slot ? pbo : pbd, qc = slot ? mine.p : pbo,
                           qdp = slot ? succ.p : pb;
@@ -1113,7 +1156,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 }
             }
             const bool     inc = si > 0;
-            const bool     itie = (slot || combo) && (rep || si == 0);
+            const bool     itie = (slot || combo) && ((MIRROR && rep) || (!rep && si == 0));
             const unsigned vm = __ballot_sync(FULL, valid), im = __ballot_sync(FULL, inc);
             const unsigned vtm = __ballot_sync(FULL, vtie), itm = __ballot_sync(FULL, itie);
             const unsigned vl = vm & 0xFu, il = im & 0xFu, vr = (vm >> 16) & 0xFu, ir = (im >> 16) & 0xFu;
@@ -1209,7 +1252,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
                 bool b2 = !top_seg;
                 if (lane == 0 && !b2)
                 {
-                    if (!*(volatile int*)&S.state[o] && !wait_other()) b2 = true;
+                    if (!other_done() && !wait_other()) b2 = true;
                     __threadfence_block();
                     if (*(volatile int*)&S.last_e[A.seg] >= 0)
                     {
@@ -1234,11 +1277,45 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
             k_new = seam_keys(take_r ? rcP : lcP, A.frame);
             const bool above = take_r ? q_above(po, pt, k_new, k_d) : q_above(po, pt, k_o, k_new);
             if (MIRROR)
-                halt = above;
+            {
+                const int j = A.seg;
+                if (!down_more && above)
+                {
+                    // q is passed: the falling walker's part ends here. Above
+                    // the first segment it publishes its last edge and waits
+                    // for its rising walker: done, or stopped early, when the
+                    // falling walker goes on down to the rising one's last edge
+                    if (j == 0)
+                        halt = true;
+                    else
+                    {
+                        S.last_e[j] = basel;
+                        S.last_o[j] = bo;
+                        S.last_d[j] = bd;
+                        __threadfence_block();
+                        *(volatile int*)&S.fpub[j] = 1;
+                        __threadfence_block();
+                        bool got = false;
+                        for (long long i = 0; i < kSeamSpin && !got; ++i)
+                        {
+                            if (*(volatile int*)&S.rstop[j])
+                                down_more = got = true;
+                            else if (*(volatile int*)&S.rdone[j] || *(volatile int*)&S.fail)
+                                halt = got = true;
+                            else
+                                __nanosleep(64);
+                        }
+                        if (!got) bad = true;
+                        __threadfence_block();
+                    }
+                }
+                if (down_more && *(volatile int*)&S.rlast_o[j] == vo && *(volatile int*)&S.rlast_d[j] == vt)
+                    taken = *(volatile int*)&S.rlast_e[j];
+            }
             else
             {
-                if (!above && !*(volatile int*)&S.state[o] && !wait_other()) bad = true;
-                if (!bad && *(volatile int*)&S.state[o])
+                if (!above && !other_done() && !wait_other()) bad = true;
+                if (!bad && other_done())
                 {
                     __threadfence_block();
                     const int j = A.seg;
@@ -1256,6 +1333,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
         bad = __shfl_sync(FULL, (int)bad, 0) != 0;
         halt = __shfl_sync(FULL, (int)halt, 0) != 0;
         taken = __shfl_sync(FULL, taken, 0);
+        if (MIRROR) down_more = __shfl_sync(FULL, (int)down_more, 0) != 0;
         if (bad || halt) break;
         if (taken >= 0)
         {
@@ -1333,6 +1411,13 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
 #endif
     if (lane == 0)
     {
+        // a falling walker that ends anywhere but at the last edge of a
+        // rising walker that stopped early leaves a gap
+        if (MIRROR && !bad && fall_done_lane0() && !(basel >= 0 && basel == *(volatile int*)&S.rlast_e[A.seg]))
+        {
+            bad = true;
+            dbg_why = 12;
+        }
         if (bad && !S.fail) fail_split(0u);
         S.ndel[w] = fill;
         if (MIRROR)
@@ -1346,6 +1431,7 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
         }
         else
         {
+            *(volatile int*)&S.rdone[A.seg] = 1;
             if (top_seg) S.top = basel;
             if (w == 0)
             {
