@@ -102,11 +102,14 @@ constexpr int kSplitFloor = 256;
 constexpr int kSplitDefaultDepth = 7;
 constexpr int kSplitDefaultPoints = 1024;
 // segments of one split merge's seam at most (two walkers each), and the
-// default node size per added segment (floor kSplitSegFloor). The block of a split merge is its walker
-// warps and an inserter warp; an SM's four sub-partitions hold 16,384
-// registers each and a block's warps are spread over them, so 7 warps of up
-// to 232 registers fit (2 a sub-partition), 9 would allow 168 at most.
-constexpr int kSplitMaxSegs = 3;
+// default node size per added segment (floor kSplitSegFloor). The block of
+// a split merge is its walker warps and an inserter warp; an SM's four
+// sub-partitions hold 16,384 registers each and a block's warps are spread
+// over them, so its 9 warps (3 on one sub-partition) get 168 registers a
+// thread (k_build_split's cap). Measured against 3 segments at 232
+// registers (7 warps, no spills): 2.6 M uniform 24.94 -> 23.71 ms a call
+// despite the spills.
+constexpr int kSplitMaxSegs = 4;
 constexpr int kSplitSegPoints = 16384;
 constexpr int kSplitSegFloor = 1024;
 // deletion lists (and spare-record ranges) of one split merge: one a

@@ -192,7 +192,7 @@ __device__ inline double seam_quantile(const unsigned long long* __restrict__ h,
 }
 
 template <int WIN>
-__global__ void __maxnreg__(232) k_build_split(Rec* __restrict__ R, int nrec, const NodeOut* __restrict__ child,
+__global__ void __maxnreg__(168) k_build_split(Rec* __restrict__ R, int nrec, const NodeOut* __restrict__ child,
     NodeOut* __restrict__ out, int m, int d, DevStatus* st, int count, SplitPlan plan, const double* __restrict__ seam,
     const unsigned long long* __restrict__ hist, const unsigned long long* __restrict__ near,
     const unsigned long long* __restrict__ box)

@@ -20,7 +20,7 @@
 //
 // The walkers never see each other's work:
 // * each record carries a tag word (Rec::pad): one bit per walker marks the
-//   edges it deleted (kSeamPre the ones deleted before the walkers), and
+//   edges it deleted (bit 8, kSeamPre, the ones deleted before the walkers), and
 //   bits 16..31 name the walker that made the edge, or the boundary;
 // * deletions only set the walker's bit: the edge stays in its rings until
 //   the merge ends, and the walker that deleted it steps over it;
@@ -89,8 +89,8 @@ namespace qdtg {
 // the seam (walker 2 j rises in segment j, walker 2 j + 1 falls)
 constexpr int       kSeamSegs = kSplitMaxSegs;
 constexpr int       kSeamWalkers = 2 * kSeamSegs;
-constexpr unsigned  kSeamDel = 0xFFu;   // deletion flags of a record's tag word, one bit per walker
-constexpr unsigned  kSeamPre = 0x80u;   // deleted before the walkers start (crosses a segment boundary)
+constexpr unsigned  kSeamPre = 0x100u;  // deleted before the walkers start (crosses a segment boundary)
+constexpr unsigned  kSeamDel = 0x1FFu;  // deletion flags of a record's tag word: one bit per walker, and kSeamPre
 constexpr int       kSeamQueue = 4;     // insertions a walker may have waiting
 constexpr long long kSeamSpin = 1ll << 24;
 
