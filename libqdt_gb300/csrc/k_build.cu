@@ -403,7 +403,7 @@ __global__ void __maxnreg__(168) k_build_split(Rec* __restrict__ R, int nrec, co
                 const double2 pr = R[gr[j] >> 1].p[gr[j] & 1], pl = R[gl[j] >> 1].p[gl[j] & 1];
                 const int     yr = R[sr[j] >> 1].next[sr[j] & 1], yl = R[sl[j] >> 1].next[sl[j] & 1];
                 *reinterpret_cast<int4*>(&R[kk].org[0]) =
-                    make_int4(vr, vl, -1, (int)(seam_gate_tag(16u * (unsigned)((1ll << d) + k), j) << 16));
+                    make_int4(vr, vl, -1, (int)(seam_gate_tag(kSeamTagStride * (unsigned)((1ll << d) + k), j) << 16));
                 R[kk].p[0] = pr;
                 R[kk].p[1] = pl;
                 R[kk].next[0] = yr;
@@ -437,7 +437,7 @@ __global__ void __maxnreg__(168) k_build_split(Rec* __restrict__ R, int nrec, co
     SeamArgs  A;
     A.R = R;
     A.nrec = nrec;
-    A.tag = 16u * (unsigned)((1ll << d) + k);
+    A.tag = kSeamTagStride * (unsigned)((1ll << d) + k);
     const long long off = plan.base[d] + (long long)split_lists(plan.segs[d]) * plan.per[d] * k;
     A.w = warp;
     A.seg = warp >> 1;

@@ -20,7 +20,7 @@
 //
 // The walkers never see each other's work:
 // * each record carries a tag word (Rec::pad): one bit per walker marks the
-//   edges it deleted (bit 8, kSeamPre, the ones deleted before the walkers), and
+//   edges it deleted (bit 12, kSeamPre, the ones deleted before the walkers), and
 //   bits 16..31 name the walker that made the edge, or the boundary;
 // * deletions only set the walker's bit: the edge stays in its rings until
 //   the merge ends, and the walker that deleted it steps over it;
@@ -89,8 +89,10 @@ namespace qdtg {
 // the seam (walker 2 j rises in segment j, walker 2 j + 1 falls)
 constexpr int       kSeamSegs = kSplitMaxSegs;
 constexpr int       kSeamWalkers = 2 * kSeamSegs;
-constexpr unsigned  kSeamPre = 0x100u;  // deleted before the walkers start (crosses a segment boundary)
-constexpr unsigned  kSeamDel = 0x1FFu;  // deletion flags of a record's tag word: one bit per walker, and kSeamPre
+static_assert(kSeamWalkers <= 12, "one deletion bit per walker below kSeamPre");
+constexpr unsigned  kSeamPre = 1u << 12;   // deleted before the walkers start (crosses a segment boundary)
+constexpr unsigned  kSeamDel = (1u << 13) - 1u;   // deletion flags of a record's tag word: one bit per walker, and kSeamPre
+constexpr unsigned  kSeamTagStride = 32;  // creator values of one merge: tag .. tag + 31
 constexpr int       kSeamQueue = 4;     // insertions a walker may have waiting
 constexpr long long kSeamSpin = 1ll << 24;
 
@@ -134,7 +136,7 @@ struct SeamArgs
 {
     Rec*       R;
     int        nrec;     // pool and spare records
-    unsigned   tag;      // 16 * node: creators tag + 1 + w; tag itself marks the segment boundaries
+    unsigned   tag;      // kSeamTagStride * node: creators tag + 1 + w, boundaries seam_gate_tag
     double2    q;        // the segment's meeting point on the seam
     int        w;        // this walker
     int        seg;      // its segment
@@ -168,11 +170,11 @@ __device__ __forceinline__ SeamKey seam_keys(double2 p, int frame)
     return frame ? SeamKey{ ~seam_key(p.x), seam_key(p.y) } : SeamKey{ seam_key(p.y), seam_key(p.x) };
 }
 
-// Creators in a record's tag word (bits 16..31), per merge (tag = 16 *
-// node): tag + 1 + w for walker w's edges (w < 8), tag + 9 + j for the
-// boundary edge where segment j begins (j >= 1, seen by the two walkers that
-// start there).
-__device__ __forceinline__ unsigned seam_gate_tag(unsigned tag, int j) { return tag + 9u + (unsigned)j; }
+// Creators in a record's tag word (bits 16..31), per merge (tag =
+// kSeamTagStride * node, nodes below 1,024): tag + 1 + w for walker w's
+// edges, tag + 16 + j for the boundary edge where segment j begins (j >= 1,
+// seen by the two walkers that start there).
+__device__ __forceinline__ unsigned seam_gate_tag(unsigned tag, int j) { return tag + 16u + (unsigned)j; }
 
 // a record walker w does not see: deleted by it (mydel: its flag, and
 // kSeamPre for a walker that starts at a segment boundary), or made in the
@@ -181,7 +183,7 @@ __device__ __forceinline__ unsigned seam_gate_tag(unsigned tag, int j) { return 
 __device__ __forceinline__ bool seam_skip(unsigned pad, unsigned mydel, unsigned tag, unsigned mytag, unsigned mygate)
 {
     const unsigned c = pad >> 16;
-    return (pad & mydel) != 0u || ((c & ~15u) == tag && c != mytag && c != mygate);
+    return (pad & mydel) != 0u || ((c & ~(kSeamTagStride - 1u)) == tag && c != mytag && c != mygate);
 }
 
 // q strictly above the cross edge po -> pt (po on the right, pt on the left
@@ -1397,15 +1399,15 @@ __device__ void seam_walk(Builder& B, SeamShared& S, const SeamArgs& A, int ldo,
     {
         const int why = __shfl_sync(FULL, dbg_why, 0) | __reduce_or_sync(FULL, (unsigned)dbg_why);
         if (lane == 0 && bad)
-            printf("split FAIL node=%u w=%d why=%d steps=%d posted=%d head=%d\n", A.tag / 16u, w, why, dbg_steps, posted,
+            printf("split FAIL node=%u w=%d why=%d steps=%d posted=%d head=%d\n", A.tag / kSeamTagStride, w, why, dbg_steps, posted,
                 *(volatile int*)&S.head[w]);
     }
 #endif
 #if QDTG_SPLIT_DEBUG
-    if (lane == 0 && A.tag / 16u < 16u)
+    if (lane == 0 && A.tag / kSeamTagStride < 16u)
         printf("split node=%u w=%d steps=%d passes=%d del=%d flush=%d stop=%d bad=%d chain=%d cyc=%lld wait=%lld "
                "lock=%lld win=%lld pred=%lld conn=%lld snap=%lld mid=%lld post=%lld spare=%d\n",
-            A.tag / 16u, w, dbg_steps, dbg_passes, dbg_del, dbg_flush, (int)stop, (int)bad, (int)done_chain,
+            A.tag / kSeamTagStride, w, dbg_steps, dbg_passes, dbg_del, dbg_flush, (int)stop, (int)bad, (int)done_chain,
             clock64() - dbg_t0, dbg_wait, dbg_lock, dbg_win, dbg_pred, dbg_conn, dbg_snap, dbg_mid, dbg_post,
             a_next - A.a0);
 #endif
