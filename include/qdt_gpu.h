@@ -94,7 +94,7 @@ QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
    GPU. No counterpart in the reference, whose merges are sequential. */
 QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);
 
-/* Seam segments of one split merge at most (1..4, default 4; a node gets
+/* Seam segments of one split merge at most (1..5, default 5; a node gets
    one more segment per segment_points points, at least 1,024, default
    16,384; on calls of at least 65,536 points).
    Segments beyond the first begin at cross edges found before the merge:

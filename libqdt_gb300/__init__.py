@@ -271,7 +271,7 @@ class Triangulation(qdt_api.Context):
         return self.lib.qdtg_set_split_merges(self.ptr, int(max_depth), int(min_points)) == 1
 
     def set_split_segments(self, max_segments: int, segment_points: int = 16384) -> bool:
-        """Seam segments of one split merge at most (1..4), one more per
+        """Seam segments of one split merge at most (1..5), one more per
         segment_points points of the node: segments beyond the first begin
         at cross edges found before the merge."""
         return self.lib.qdtg_set_split_segments(self.ptr, int(max_segments), int(segment_points)) == 1

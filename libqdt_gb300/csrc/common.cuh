@@ -105,11 +105,11 @@ constexpr int kSplitDefaultPoints = 1024;
 // default node size per added segment (floor kSplitSegFloor). The block of
 // a split merge is its walker warps and an inserter warp; an SM's four
 // sub-partitions hold 16,384 registers each and a block's warps are spread
-// over them, so its 9 warps (3 on one sub-partition) get 168 registers a
+// over them, so its 11 warps (3 on a sub-partition) get 168 registers a
 // thread (k_build_split's cap). Measured against 3 segments at 232
 // registers (7 warps, no spills): 2.6 M uniform 24.94 -> 23.71 ms a call
-// despite the spills.
-constexpr int kSplitMaxSegs = 4;
+// with 4 segments despite the spills, 22.78 ms with 5.
+constexpr int kSplitMaxSegs = 5;
 constexpr int kSplitSegPoints = 16384;
 constexpr int kSplitSegFloor = 1024;
 // deletion lists (and spare-record ranges) of one split merge: one a

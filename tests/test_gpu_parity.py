@@ -275,7 +275,7 @@ _GENERAL = ("uniform_1m", "uniform_2p6m", "gauss", "blobs", "line")
 def test_split_segments_same_result(lib):
     """Seams cut into segments at boundary edges (mutually nearest vertices
     of the two halves, the children's edges that cross them deleted first),
-    two walkers a segment: for 1, 2 and 4 segments the canonical triangles
+    two walkers a segment: for 1, 2 and 5 segments the canonical triangles
     and representatives of the one-walker build, on every kind of input, and
     identical arrays on a second run. On input in general position the
     merges use the segments without falling back; on degenerate input (a
@@ -291,7 +291,7 @@ def test_split_segments_same_result(lib):
             assert t.execute(p) == 0, name
             want_t = O.canonical(t.triangles_array())
             want_r = t.rep_array().copy()
-        for segs in (1, 2, 4):
+        for segs in (1, 2, 5):
             runs = []
             for _ in range(2):
                 with G.Triangulation(lib) as t:
@@ -315,9 +315,9 @@ def test_split_segments_same_result(lib):
 def test_split_segments_knob(lib):
     with G.Triangulation(lib) as t:
         assert not t.set_split_segments(0)
-        assert not t.set_split_segments(5)
+        assert not t.set_split_segments(6)
         assert not t.set_split_segments(2, 1023)
-        for segs in (1, 2, 3, 4):
+        for segs in (1, 2, 3, 4, 5):
             assert t.set_split_segments(segs)
 
 
