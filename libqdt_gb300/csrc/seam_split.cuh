@@ -93,7 +93,10 @@ static_assert(kSeamWalkers <= 12, "one deletion bit per walker below kSeamPre");
 constexpr unsigned  kSeamPre = 1u << 12;   // deleted before the walkers start (crosses a segment boundary)
 constexpr unsigned  kSeamDel = (1u << 13) - 1u;   // deletion flags of a record's tag word: one bit per walker, and kSeamPre
 constexpr unsigned  kSeamTagStride = 32;  // creator values of one merge: tag .. tag + 31
-constexpr int       kSeamQueue = 4;     // insertions a walker may have waiting
+// insertions a walker may have waiting (2: fewer registers held for the
+// pending anchors at the 168-register cap, 2.6 M 22.83 -> 22.61 ms a call
+// against 4)
+constexpr int       kSeamQueue = 2;
 constexpr long long kSeamSpin = 1ll << 24;
 
 // A ring insertion a walker asks for: the new edge e = 2 k from vo to vt
