@@ -117,6 +117,38 @@ def large_specs():
     return specs
 
 
+def limit_spec():
+    """The reference's size limit (kMaxPoints = 1e8, libqdt/wrapper.hxx:15):
+    uniform points, one call."""
+    return {"name": "uniform_100m", "gen": "uniform", "n": 100_000_000, "seed": 5}
+
+
+def canonical_digest32(tris: np.ndarray, chunk: int = 1 << 24) -> str:
+    """SHA-256 of oracle.canonical(tris) as int64 rows, computed with 32-bit
+    columns and a lexicographic sort of them (indices below 2^31), hashed in
+    chunks: the same digest with a fraction of the memory at 1e8 points."""
+    import hashlib
+    t = np.asarray(tris).reshape(-1, 3)
+    h = hashlib.sha256()
+    if t.shape[0] == 0:
+        return h.hexdigest()
+    t = t.astype(np.int32, copy=False)
+    k = np.argmin(t, axis=1).astype(np.int8)
+    r = np.empty_like(t)
+    for j in range(3):
+        r[:, j] = np.choose((k + j) % 3, (t[:, 0], t[:, 1], t[:, 2]))
+    del k
+    if int(r.max()) < (1 << 27):
+        # the first two indices identify a triangle of a triangulation (a
+        # directed edge bounds one triangle): one 54-bit key, the same order
+        order = np.argsort((r[:, 0].astype(np.uint64) << np.uint64(27)) | r[:, 1].astype(np.uint64), kind="stable")
+    else:
+        order = np.lexsort((r[:, 2], r[:, 1], r[:, 0]))
+    for s in range(0, order.shape[0], chunk):
+        h.update(r[order[s:s + chunk]].astype(np.int64).tobytes())
+    return h.hexdigest()
+
+
 # The many-set workload at its stated size: 4,096 sets, sizes log-uniform in
 # [16, 65,536], square or disk, 10 % snapped to a 256 x 256 grid.
 CONFIG_B = {"count": 4096, "lo": 16, "hi": 65536, "seed": 23}

@@ -86,6 +86,50 @@ def test_large_workloads_equal_reference(lib, spec):
     assert _digest(used) == spec["serial"]["used_digest"]
 
 
+def _canonical_digest_on_gpu(tris):
+    """tests/golden/cases.canonical_digest32 (the SHA-256 of oracle.canonical
+    as int64 rows) with the rotation and the sort done by torch on the GPU:
+    the same bytes hashed, in seconds at 2e8 triangles."""
+    torch = pytest.importorskip("torch")
+    t = torch.from_numpy(np.ascontiguousarray(tris).astype(np.int64)).cuda()
+    k = torch.argmin(t, dim=1)
+    idx = (k[:, None] + torch.arange(3, device=t.device)[None, :]) % 3
+    r = torch.gather(t, 1, idx)
+    del t, k, idx
+    assert int(r.max()) < (1 << 27)
+    order = torch.argsort(r[:, 0] * (1 << 27) + r[:, 1], stable=True)
+    r = r[order]
+    del order
+    h = hashlib.sha256()
+    step = 1 << 24
+    for i in range(0, r.shape[0], step):
+        h.update(r[i:i + step].cpu().numpy().tobytes())
+    del r
+    torch.cuda.empty_cache()
+    return h.hexdigest()
+
+
+def test_reference_size_limit(lib):
+    """At the reference's own size limit (kMaxPoints = 1e8 points,
+    libqdt/wrapper.hxx:15) one call gives the reference's triangles and
+    used points: digests made by the reference itself, serial call
+    (tests/golden/limit.json, make_limit.py)."""
+    with open(os.path.join(GOLDEN, "limit.json")) as f:
+        spec = json.load(f)["case"]
+    pts = C.make_large(spec)
+    assert pts.shape[0] == 100_000_000
+    with G.Triangulation(lib) as t:
+        assert t.execute(pts) == 0
+        tris = t.triangles_array()
+        rep = t.rep_array()
+    del pts
+    assert tris.shape[0] == spec["serial"]["ntri"]
+    assert _canonical_digest_on_gpu(tris) == spec["serial"]["tri_digest"]
+    del tris
+    used = (rep == np.arange(rep.shape[0], dtype=rep.dtype)).astype(np.uint8)
+    assert _digest(used) == spec["serial"]["used_digest"]
+
+
 def _random_sets():
     rng = np.random.default_rng(2024)
     out = []
