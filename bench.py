@@ -361,11 +361,31 @@ def run_gb300(args):
             line["handle"] = run_handle_leg(lib, pts, args)
         if "stress" in legs:
             line["stress"] = run_stress_leg(lib, args, flush)
+        line["summary"] = summarize(line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def summarize(line):
+    """The legs' headline figures in one small object at the end of the line
+    (the line's tail is what a log keeps): single device and e2e Mpts/s, the
+    batched ones, serving p50/p99 per rate, the stress rows' Mpts/s."""
+    out = {"single": line.get("value"), "single_e2e": (line.get("e2e") or {}).get("value")}
+    b = line.get("batched")
+    if b:
+        out["batched"] = b.get("value")
+        out["batched_e2e"] = (b.get("e2e") or {}).get("value")
+        out["batched_vs_plain"] = b.get("speedup_e2e_vs_plain")
+    sv = line.get("serving")
+    if sv:
+        out["serving_p50_p99_ms"] = {str(int(r["rate_per_s"])): [r["p50_ms"], r["p99_ms"]] for r in sv.get("rates", [])}
+    st = line.get("stress")
+    if st:
+        out["stress"] = {r["workload"]: r["value"] for r in st}
+    return out
 
 
 def run_batched_leg(lib, args, flush):
