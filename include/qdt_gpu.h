@@ -36,7 +36,7 @@ typedef struct qdtg_run_info
     int                merge_window;    /* candidate window of the warp merges (1 or 2; 0 = none ran) */
     int                wide_exact;      /* 1: a predicate needed the widest exact tier and the build ran
                                            again with the kernels that have it */
-    int                split_depth;     /* deepest depth whose merges ran with two walkers (-1: none) */
+    int                split_depth;     /* deepest depth whose merges ran as split merges (-1: none) */
     int                split_rerun;     /* 1: a split merge could not finish and the build ran again
                                            (with one seam segment a merge, else one walker) */
     int                split_segments;  /* the most seam segments of a split merge in the last pass */
@@ -84,12 +84,14 @@ QDT_API int qdtg_set_split_tail(qdt_t* ptr, int on);
 QDT_API int qdtg_set_side_prefetch(qdt_t* ptr, int on);
 
 /* The merges at the top of the build -- depths 0..max_depth (at most 9)
-   whose nodes hold at least min_points points (at least 256) -- run with
-   two walkers each: the reference's rising merge from the lower common
-   tangent and its mirror image from the upper one, which meet at a point of
-   the seam. A merge whose falling walker meets cocircular or collinear
-   points is finished by the rising one, so the triangulation is the same
-   as with one walker per merge (max_depth -1). Defaults 7 and 1,024.
+   whose nodes hold at least min_points points (at least 256) -- run as
+   split merges: their seam is cut into segments (qdtg_set_split_segments),
+   each walked by two walkers, the reference's rising merge from the
+   segment's lower end and its mirror image from its upper end, which meet
+   at a point of the seam. A falling walker that meets cocircular or
+   collinear points hands its part to the rising one, so the triangulation
+   is the same as with one walker per merge (max_depth -1). Defaults 7 and
+   1,024.
    Returns 1, or 0 for a NULL context, values out of range or no usable
    GPU. No counterpart in the reference, whose merges are sequential. */
 QDT_API int qdtg_set_split_merges(qdt_t* ptr, int max_depth, int min_points);

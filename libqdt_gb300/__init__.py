@@ -266,7 +266,7 @@ class Triangulation(qdt_api.Context):
         return self.lib.qdtg_set_side_prefetch(self.ptr, int(bool(on))) == 1
 
     def set_split_merges(self, max_depth: int, min_points: int = 8192) -> bool:
-        """Two walkers per merge at depths 0..max_depth (nodes of at least
+        """Split merges (seam segments, two walkers each) at depths 0..max_depth (nodes of at least
         min_points points); max_depth -1: one walker per merge."""
         return self.lib.qdtg_set_split_merges(self.ptr, int(max_depth), int(min_points)) == 1
 

@@ -499,9 +499,9 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     info_.window = b.window;
     info_.wide = 0;
     info_.split_rerun = 0;
-    // the top merges with two walkers, except on lattice-like input (the
-    // window-1 test above): there nearly every in-circle test is a tie, the
-    // falling walker stops at its first, and the rising one walks alone
+    // the top merges as split merges, except on lattice-like input (the
+    // window-1 test above): there nearly every in-circle test is a tie, a
+    // falling walker stops at its first, and the rising ones walk alone
     {
         int* lists = b.split.lists;
         if (split_depth_ >= 0 && b.window != 1)

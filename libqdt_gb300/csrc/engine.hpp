@@ -106,7 +106,7 @@ struct RunInfo
     int                    launches = 0;
     int                    window = 0;   // warp merges' candidate window of the last call
     int                    wide = 0;     // the build ran again with the widest exact tier
-    int                    split_depth = -1;   // deepest depth merged by two walkers (-1: none)
+    int                    split_depth = -1;   // deepest depth merged as split merges (-1: none)
     int                    split_rerun = 0;    // a split merge failed and the build ran again (fewer segments, or without them)
     int                    split_segments = 0; // the most seam segments of a split merge in the last pass
 };
@@ -214,7 +214,7 @@ public:
     // no other engine is running a call (default on)
     void            set_side_prefetch(bool on) { side_prefetch_ = on; }
     // merges of depth at most max_depth whose nodes hold at least min_points
-    // points run with two walkers (seam_split.cuh); max_depth -1: none
+    // points run as split merges (seam_split.cuh); max_depth -1: none
     void            set_split(int max_depth, int min_points)
     {
         split_depth_ = max_depth;

@@ -64,7 +64,7 @@ struct BuildBuffers
     // merges of this one (none: the prefetch runs in line)
     cudaStream_t   side = nullptr;
     cudaEvent_t    fork = nullptr, join = nullptr;
-    SplitPlan      split;               // the top merges with two walkers (depth -1: none)
+    SplitPlan      split;               // the top merges as split merges (depth -1: none)
     unsigned long long* seam_hist = nullptr; // kSeamBins per node of the split depths (2^(kSplitMaxDepth+1) nodes)
     // per node of the split depths, bin along the seam and side: the
     // half-edge leaving the vertex nearest to the cut (distance as float
