@@ -265,9 +265,10 @@ class Triangulation(qdt_api.Context):
     def set_side_prefetch(self, on: bool) -> bool:
         return self.lib.qdtg_set_side_prefetch(self.ptr, int(bool(on))) == 1
 
-    def set_split_merges(self, max_depth: int, min_points: int = 8192) -> bool:
-        """Split merges (seam segments, two walkers each) at depths 0..max_depth (nodes of at least
-        min_points points); max_depth -1: one walker per merge."""
+    def set_split_merges(self, max_depth: int, min_points: int = 1024) -> bool:
+        """Split merges (seam segments, two walkers each) at depths
+        0..max_depth, nodes of at least min_points points (the library's
+        defaults: 7 and 1,024); max_depth -1: one walker per merge."""
         return self.lib.qdtg_set_split_merges(self.ptr, int(max_depth), int(min_points)) == 1
 
     def set_split_segments(self, max_segments: int, segment_points: int = 16384) -> bool:
