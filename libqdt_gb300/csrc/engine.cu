@@ -524,11 +524,12 @@ int Engine::pipeline(size_t n, bool host_io, uint32_t* host_tris, size_t host_tr
     };
     info_.split_segments = plan_segs();
     // the graph key's first word: m, and above it the plan's segments a
-    // depth (2 bits each)
+    // depth (3 bits each)
+    static_assert(kSplitMaxSegs < 8 && 32 + 3 * (kSplitMaxDepth + 1) <= 64, "segments fit the graph key");
     auto key_of_m = [&] {
         uint64_t k = (uint64_t)m;
         for (int d = 0; d <= b.split.depth && d <= kSplitMaxDepth; ++d)
-            k |= (uint64_t)(b.split.segs[d] & 3) << (32 + 2 * d);
+            k |= (uint64_t)(b.split.segs[d] & 7) << (32 + 3 * d);
         return k;
     };
     // the stages after the count depend only on m and the knobs: one CUDA
