@@ -165,3 +165,61 @@ def test_locate_and_batch_insert_host_checks(lib):
         assert lib.qdtg_trace_constraints(t.ptr, None, 1, None, None) == Q.QDT_ERR_NULL_ARGUMENT
         st, s, c = t.trace_constraints(np.array([[0, 1], [2, 2]]))
         assert st == Q.QDT_OK and (s == Q.QDT_ERR_INVALID_INDEX).all() and (c == 0).all()
+
+
+def _c_layout(tmp_path, struct, fields):
+    """sizeof and offsetof of a header struct, printed by a C program built
+    against include/qdt.h and include/qdt_gpu.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("cc") or shutil.which("gcc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    body = "".join(f'    printf("%zu\\n", offsetof({struct}, {f}));\n' for f in fields)
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"qdt.h\"\n#include \"qdt_gpu.h\"\n"
+                   f"int main(void)\n{{\n    printf(\"%zu\\n\", sizeof({struct}));\n{body}    return 0;\n}}\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    return int(out[0]), [int(x) for x in out[1:]]
+
+
+@pytest.mark.parametrize("name", ["run_info", "server_config", "server_stats", "vec2d", "edge"])
+def test_ctypes_structs_match_the_headers(tmp_path, name):
+    """Every struct the Python binding passes through the C ABI has the
+    header's size and field offsets."""
+    from libqdt_gb300 import serving as S
+    py, c = {"run_info": (G.RunInfo, "qdtg_run_info"), "server_config": (S.ServerConfig, "qdtg_server_config"),
+             "server_stats": (S.ServerStats, "qdtg_server_stats"), "vec2d": (Q.Vec2d, "qdt_vec2d"),
+             "edge": (Q.Edge, "qdt_edge")}[name]
+    fields = [f for f, _ in py._fields_]
+    size, offsets = _c_layout(tmp_path, c, fields)
+    assert ctypes.sizeof(py) == size
+    assert [getattr(py, f).offset for f in fields] == offsets
+
+
+def test_filter_stats_size_matches_the_header(tmp_path):
+    size, _ = _c_layout(tmp_path, "qdtg_filter_stats", [])
+    assert size == 3 * 4 * 2 * 8
+
+
+def test_split_knob_argument_checks(lib):
+    """qdtg_set_split_merges and qdtg_set_split_segments reject a NULL
+    context and out-of-range values before they touch the GPU."""
+    assert lib.qdtg_set_split_merges(None, 7, 1024) == 0
+    assert lib.qdtg_set_split_segments(None, 2, 16384) == 0
+    with G.Triangulation(lib) as t:
+        assert lib.qdtg_set_split_merges(t.ptr, -2, 1024) == 0
+        assert lib.qdtg_set_split_merges(t.ptr, 10, 1024) == 0     # deepest split depth is 9
+        assert lib.qdtg_set_split_merges(t.ptr, 7, 255) == 0       # at least 256 points a node
+        assert lib.qdtg_set_split_segments(t.ptr, 0, 16384) == 0
+        assert lib.qdtg_set_split_segments(t.ptr, 6, 16384) == 0   # at most 5 segments a merge
+        assert lib.qdtg_set_split_segments(t.ptr, 2, 1023) == 0    # at least 1024 points a segment
+        info = G.RunInfo()
+        assert lib.qdtg_get_run_info(t.ptr, ctypes.byref(info)) == 1
+        assert info.n == 0 and info.triangles == 0 and info.split_segments == 0
+        assert lib.qdtg_get_run_info(t.ptr, None) == 0
+    assert lib.qdtg_get_run_info(None, ctypes.byref(G.RunInfo())) == 0
