@@ -573,8 +573,9 @@ bool insertion_cavity(Context& c, Mesh& M, int in, int seen, double x, double y,
         else
             for (int e : sees)
             {
+                // a constrained hull edge hides the triangle behind it
                 const int t = M.h[e].tri;
-                if (!taken(t) && !is_excluded(t) && circle_holds(M, t, x, y) > 0) take(t);
+                if (!M.h[e].cons && !taken(t) && !is_excluded(t) && circle_holds(M, t, x, y) > 0) take(t);
             }
         for (size_t i = 0; i < cav.size(); ++i)
         {
@@ -696,6 +697,10 @@ int mesh_insert_point(Context& c, double x, double y, bool, int hint)
         if (q.ext >= 0) M.h[q.ext].twin = e0;
         M.h[e1].twin = M.h[e2].twin = -1;
         M.h[e1].cons = M.h[e2].cons = 0;
+        // both ends get a half-edge that survives: the old one may lie in a
+        // cavity slot now reused (the last end of an open border, after a
+        // point outside the hull, starts no border edge)
+        M.v[q.b].he = e1;
         M.v[q.a].he = e0;
         into.emplace_back(q.b, e1);
         out.emplace_back(q.a, e2);

@@ -1,0 +1,123 @@
+"""The handle operations' host code (mesh.cu) against the reference library
+itself, on operation sequences that are not in the committed fixtures.
+
+Where the reference was compiled from its own sources into oracle/_ref, each
+case triangulates fresh seeded points in both libraries (ours is loaded with
+the oracle's triangulation through qdtg_set_triangulation, so no GPU is
+needed), applies the same insertions and constraints in the same order, and
+requires equal statuses, returned indices, used flags and triangle counts;
+equal triangle sets where the input is in general position (the constrained
+Delaunay triangulation is unique there), and everywhere a valid constrained
+Delaunay triangulation that holds every accepted constraint (as the pieces
+later insertions on it split it into). Skipped where the reference is not compiled.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import libqdt_gb300 as G
+from libqdt_gb300 import qdt_api as Q
+from oracle import delaunay_check as D
+from oracle import oracle as O
+from tests import mesh_check as MC
+
+pytestmark = pytest.mark.skipif(
+    not (O.reference_available() and os.path.exists(os.path.join(O.REF_DIR, "libqdt_dump_ref.so"))),
+    reason="the reference is not compiled here (oracle/_ref)")
+
+
+@pytest.fixture(scope="module")
+def libs():
+    from tests.golden import make_golden as M
+    return G.load(), Q.load(O.REF_LIB_PATH), M.load_dump()
+
+
+def _case(seed):
+    """(points, ops, general position) for one seed."""
+    rng = np.random.default_rng(seed)
+    kind = seed % 4
+    n = int(rng.integers(3, 400))
+    ops = []
+    if kind == 0:      # uniform doubles, insertions inside and around the hull
+        p = rng.random((n, 2))
+        for _ in range(int(rng.integers(1, 60))):
+            if rng.random() < 0.6:
+                ops.append(("insert", float(rng.random() * 1.4 - 0.2), float(rng.random() * 1.4 - 0.2)))
+            else:
+                ops.append(("constraint", int(rng.integers(0, n + 3)), int(rng.integers(0, n + 3))))
+        return p, ops, True
+    # integer points: duplicates, insertions on vertices, edges and outside
+    R = int(rng.choice([4, 10, 40]))
+    p = rng.integers(0, R, size=(n, 2)).astype(np.float64)
+    for _ in range(int(rng.integers(1, 60))):
+        r = rng.random()
+        if r < 0.2:
+            q = p[int(rng.integers(0, n))]
+            ops.append(("insert", float(q[0]), float(q[1])))
+        elif r < 0.5:
+            q = rng.integers(-2, R + 2, size=2) + (0.5 if kind == 2 else 0.0) * rng.integers(0, 2, size=2)
+            ops.append(("insert", float(q[0]), float(q[1])))
+        else:
+            ops.append(("constraint", int(rng.integers(0, n + 3)), int(rng.integers(0, n + 3))))
+    return p, ops, False
+
+
+def _split_constraints(t, cons):
+    """The accepted constraints as the edges they consist of now: a point
+    inserted later on a constrained edge splits it. For the integer cases
+    (coordinates on a half-integer grid, so twice them are exact integers)."""
+    rep = t.rep_array()
+    P = np.array([t.point(i)[1] for i in range(t.points_size())])
+    Q2 = np.rint(2 * P).astype(np.int64)
+    assert np.array_equal(Q2, 2 * P)
+    V = np.unique(rep)
+    out = []
+    for a, b in cons:
+        a, b = int(rep[a]), int(rep[b])
+        d = Q2[b] - Q2[a]
+        r = Q2[V] - Q2[a]
+        s = r[:, 0] * d[0] + r[:, 1] * d[1]
+        on = (d[0] * r[:, 1] - d[1] * r[:, 0] == 0) & (s > 0) & (s < d[0] * d[0] + d[1] * d[1])
+        chain = [a] + [int(v) for v in V[on][np.argsort(s[on])]] + [b]
+        out += list(zip(chain[:-1], chain[1:]))
+    return out
+
+
+def _reference(lib, dump, pts, ops, par):
+    with Q.Context(lib) as c:
+        assert c.execute(pts, parallel=par) == 0
+        st = MC.run_ops(c, ops, par)
+        tris = np.zeros((c.triangles_size(), 3), dtype=np.int64)
+        dump.qdt_dump_triangles(c.ptr, tris.ctypes.data)
+        used = np.zeros(c.points_size(), dtype=np.uint8)
+        dump.qdt_dump_used(c.ptr, used.ctypes.data)
+    return st, O.canonical(tris), used
+
+
+@pytest.mark.parametrize("block", range(4))
+def test_mesh_operations_equal_reference_on_fresh_sequences(libs, block):
+    ours, ref, dump = libs
+    checked = 0
+    for seed in range(880000 + 500 * block, 880000 + 500 * (block + 1)):
+        pts, ops, general = _case(seed)
+        r = O.triangulate(pts)
+        if r.tris.shape[0] == 0:
+            continue   # collinear points: an insertion re-runs the batch call, on the GPU
+        par = bool(seed & 1)
+        want_st, want_tris, want_used = _reference(ref, dump, pts, ops, par)
+        with G.Triangulation(ours) as t:
+            assert t.set_triangulation(pts, r.tris, r.rep) == Q.QDT_OK
+            st = MC.run_ops(t, ops, par)
+            assert np.array_equal(st, want_st), (seed, st, want_st)
+            used = np.array([t.point_is_used(i) for i in range(t.points_size())], dtype=np.uint8)
+            assert np.array_equal(used, want_used), seed
+            got = O.canonical(t.triangles_array())
+            assert got.shape == want_tris.shape, seed
+            if general:
+                assert np.array_equal(got, want_tris), seed
+            cons = MC.accepted_constraints(ops, st)
+            res = MC.constrained_valid(t, cons if general else _split_constraints(t, cons))
+            assert D.ok(res), (seed, res)
+        checked += 1
+    assert checked > 450
