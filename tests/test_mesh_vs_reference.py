@@ -4,8 +4,8 @@ itself, on operation sequences that are not in the committed fixtures.
 Where the reference was compiled from its own sources into oracle/_ref, each
 case triangulates fresh seeded points in both libraries (ours is loaded with
 the oracle's triangulation through qdtg_set_triangulation, so no GPU is
-needed), applies the same insertions and constraints in the same order, and
-requires equal statuses, returned indices, used flags and triangle counts;
+needed), applies the same insertions and constraints in the same order, then one
+qdt_insert_constraints_batch call, and requires equal statuses, returned indices, used flags and triangle counts;
 equal triangle sets where the input is in general position (the constrained
 Delaunay triangulation is unique there), and everywhere a valid constrained
 Delaunay triangulation that holds every accepted constraint (as the pieces
@@ -84,10 +84,25 @@ def _split_constraints(t, cons):
     return out
 
 
-def _reference(lib, dump, pts, ops, par):
+def _batch_edges(seed, m):
+    """The qdt_insert_constraints_batch call that ends a sequence: random
+    end points among the m points (some invalid, some equal)."""
+    rng = np.random.default_rng(seed + 7)
+    return rng.integers(0, m + 2, size=(int(rng.integers(0, 30)), 2))
+
+
+def _apply(c, ops, par, edges):
+    """The operations, then one batch of constraints: every status as one
+    array (the batch's return value, then its per-edge results)."""
+    st = MC.run_ops(c, ops, par)
+    bst, bres = c.insert_constraints_batch(edges)
+    return st, np.concatenate([[bst], bres]).astype(np.int64)
+
+
+def _reference(lib, dump, pts, ops, par, edges):
     with Q.Context(lib) as c:
         assert c.execute(pts, parallel=par) == 0
-        st = MC.run_ops(c, ops, par)
+        st = _apply(c, ops, par, edges)
         tris = np.zeros((c.triangles_size(), 3), dtype=np.int64)
         dump.qdt_dump_triangles(c.ptr, tris.ctypes.data)
         used = np.zeros(c.points_size(), dtype=np.uint8)
@@ -105,11 +120,13 @@ def test_mesh_operations_equal_reference_on_fresh_sequences(libs, block):
         if r.tris.shape[0] == 0:
             continue   # collinear points: an insertion re-runs the batch call, on the GPU
         par = bool(seed & 1)
-        want_st, want_tris, want_used = _reference(ref, dump, pts, ops, par)
+        edges = _batch_edges(seed, pts.shape[0] + len(ops))
+        (want_st, want_bst), want_tris, want_used = _reference(ref, dump, pts, ops, par, edges)
         with G.Triangulation(ours) as t:
             assert t.set_triangulation(pts, r.tris, r.rep) == Q.QDT_OK
-            st = MC.run_ops(t, ops, par)
+            st, bst = _apply(t, ops, par, edges)
             assert np.array_equal(st, want_st), (seed, st, want_st)
+            assert np.array_equal(bst, want_bst), (seed, bst, want_bst)
             used = np.array([t.point_is_used(i) for i in range(t.points_size())], dtype=np.uint8)
             assert np.array_equal(used, want_used), seed
             got = O.canonical(t.triangles_array())
@@ -117,6 +134,7 @@ def test_mesh_operations_equal_reference_on_fresh_sequences(libs, block):
             if general:
                 assert np.array_equal(got, want_tris), seed
             cons = MC.accepted_constraints(ops, st)
+            cons += [(int(a), int(b)) for (a, b), s in zip(edges, bst[1:]) if s == 0]
             res = MC.constrained_valid(t, cons if general else _split_constraints(t, cons))
             assert D.ok(res), (seed, res)
         checked += 1
