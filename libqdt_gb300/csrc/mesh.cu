@@ -721,10 +721,15 @@ int mesh_insert_point(Context& c, double x, double y, bool, int hint)
         }
     }
     M.v[p].he = first_spoke;
-    // the two halves of a split constrained edge stay constrained
+    // the two halves of a split constrained edge stay constrained; on the
+    // hull one half is an outgoing spoke only (p -> split end, no twin)
     if (split_a >= 0)
+    {
         for (const auto& s : into)
             if (s.first == split_a || s.first == split_b) set_constrained(M, s.second);
+        for (const auto& s : out)
+            if (s.first == split_a || s.first == split_b) set_constrained(M, s.second);
+    }
     M.last = M.t2h[M.h[first_spoke].tri];
     return QDT_OK;
 }

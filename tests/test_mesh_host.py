@@ -115,6 +115,22 @@ def test_insert_on_constrained_edge_splits_it(lib):
         assert t.insert_constraint(1, 3) == Q.QDT_ERR_THROUGH_POINT        # (2,0)-(0,2) runs through (1,1)
 
 
+def test_split_constrained_hull_edge_keeps_both_halves(lib):
+    """A point on a constrained hull edge splits it into two constrained
+    halves; a point added outside then sees both, hidden behind them, and
+    a segment from it across either half is refused."""
+    sq = np.array([[0.0, 0.0], [4.0, 0.0], [4.0, 4.0], [0.0, 4.0], [2.0, 2.5]])
+    with loaded(lib, sq) as t:
+        assert t.insert_constraint(0, 1) == 0                      # the bottom hull edge
+        assert t.insert_point(2.0, 0.0) == (0, 5)                  # on it
+        assert t.insert_point(2.0, -3.0) == (0, 6)                 # below the hull
+        res = MC.constrained_valid(t, [(0, 5), (5, 1)])
+        assert D.ok(res), res
+        assert t.insert_constraint(6, 2) == Q.QDT_ERR_CROSSES_CONSTRAINT   # across (2,0)-(4,0)
+        assert t.insert_constraint(6, 3) == Q.QDT_ERR_CROSSES_CONSTRAINT   # across (0,0)-(2,0)
+        assert t.insert_constraint(6, 4) == Q.QDT_ERR_THROUGH_POINT        # through (2,0)
+
+
 def test_set_triangulation_checks(lib):
     pts = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 0.0]])
     with G.Triangulation(lib) as t:
