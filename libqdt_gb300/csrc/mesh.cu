@@ -842,13 +842,23 @@ int fill_channel(Context& c, Mesh& M, int u, int w, const Channel& ch)
         int      ext, cons;
     };
     std::vector<Outer> outer;
+    // Constrained edges with channel triangles on both sides. The segment
+    // crosses none of them (open_channel refuses that): each joins a vertex
+    // whose whole fan lies in the channel to a neighbour on the same side of
+    // the segment, an antenna of that side's pseudo-polygon. The fill keeps
+    // the edge (a polygon edge); it must keep the flag too.
+    std::vector<uint64_t> antennas;
     for (int t : ch.tris)
     {
         const int e0 = M.t2h[t];
         for (int k = 0, e = e0; k < 3; ++k, e = nxt(M, e))
         {
             const int tw = M.h[e].twin;
-            if (tw >= 0 && M.mark[M.h[tw].tri] == stamp) continue;
+            if (tw >= 0 && M.mark[M.h[tw].tri] == stamp)
+            {
+                if (M.h[e].cons) antennas.push_back(edge_key(M.h[e].org, dst(M, e)));
+                continue;
+            }
             outer.push_back(Outer{ edge_key(M.h[e].org, dst(M, e)), tw, M.h[e].cons });
         }
     }
@@ -889,6 +899,12 @@ int fill_channel(Context& c, Mesh& M, int u, int w, const Channel& ch)
         M.h[f.second].twin = o->ext;
         M.h[f.second].cons = o->cons;
         if (o->ext >= 0) M.h[o->ext].twin = f.second;
+    }
+    for (const uint64_t k : antennas)
+    {
+        const auto f = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(k, INT_MIN));
+        if (f == fresh.end() || f->first != k) return QDT_ERR_INTERNAL;
+        set_constrained(M, f->second);
     }
     const auto uw = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(edge_key(u, w), INT_MIN));
     if (uw == fresh.end() || uw->first != edge_key(u, w)) return QDT_ERR_INTERNAL;

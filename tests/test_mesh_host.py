@@ -131,6 +131,25 @@ def test_split_constrained_hull_edge_keeps_both_halves(lib):
         assert t.insert_constraint(6, 4) == Q.QDT_ERR_THROUGH_POINT        # through (2,0)
 
 
+def test_constraint_around_a_constrained_antenna(lib):
+    """(0, 3.5) has three neighbours, the corners of the triangle around it;
+    the segment (-20,4)-(20,4) passes just above it and crosses its whole
+    fan. The constrained edge (0,0)-(0,3.5), which it does not cross, stays
+    an edge and stays constrained (a segment across it is refused), as in
+    the reference."""
+    pts = np.array([[0, 0], [-5, 10], [5, 10], [0, 3.5], [-20, 4], [20, 4], [0, -6], [0, 16]], dtype=np.float64)
+    with loaded(lib, pts) as t:
+        nb = {int(x) for tri in t.triangles_array() for x in tri if 3 in tri} - {3}
+        assert nb == {0, 1, 2}
+        assert t.insert_constraint(0, 3) == 0
+        assert t.insert_constraint(4, 5) == 0
+        assert t.insert_point(-1.0, 1.0) == (0, 8)
+        assert t.insert_point(1.0, 2.0) == (0, 9)
+        assert t.insert_constraint(8, 9) == Q.QDT_ERR_CROSSES_CONSTRAINT
+        res = MC.constrained_valid(t, [(0, 3), (4, 5)])
+        assert D.ok(res), res
+
+
 def test_set_triangulation_checks(lib):
     pts = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 0.0]])
     with G.Triangulation(lib) as t:

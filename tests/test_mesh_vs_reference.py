@@ -36,9 +36,27 @@ def libs():
 def _case(seed):
     """(points, ops, general position) for one seed."""
     rng = np.random.default_rng(seed)
-    kind = seed % 4
+    kind = seed % 5
     n = int(rng.integers(3, 400))
     ops = []
+    if kind == 4:      # a few integer points; insertions at midpoints of point pairs, repeats, far points
+        p = rng.integers(0, int(rng.integers(2, 17)), size=(int(rng.integers(3, 12)), 2)).astype(np.float64)
+        allp = [tuple(x) for x in p]
+        for _ in range(int(rng.integers(1, 200))):
+            r = rng.random()
+            if r < 0.45:
+                if r < 0.3:
+                    a, b = allp[int(rng.integers(0, len(allp)))], allp[int(rng.integers(0, len(allp)))]
+                    q = ((a[0] + b[0]) / 2, (a[1] + b[1]) / 2)
+                elif r < 0.37:
+                    q = tuple(float(v) for v in rng.integers(-50, 50, size=2))
+                else:
+                    q = allp[int(rng.integers(0, len(allp)))]
+                ops.append(("insert", float(q[0]), float(q[1])))
+                allp.append(q)
+            else:
+                ops.append(("constraint", int(rng.integers(0, len(allp))), int(rng.integers(0, len(allp)))))
+        return p, ops, False
     if kind == 0:      # uniform doubles, insertions inside and around the hull
         p = rng.random((n, 2))
         for _ in range(int(rng.integers(1, 60))):
@@ -66,11 +84,12 @@ def _case(seed):
 def _split_constraints(t, cons):
     """The accepted constraints as the edges they consist of now: a point
     inserted later on a constrained edge splits it. For the integer cases
-    (coordinates on a half-integer grid, so twice them are exact integers)."""
+    (coordinates below 64 in magnitude on a grid of 2^-20: scaled by 2^20
+    they are exact integers, and the products below fit in 64 bits)."""
     rep = t.rep_array()
     P = np.array([t.point(i)[1] for i in range(t.points_size())])
-    Q2 = np.rint(2 * P).astype(np.int64)
-    assert np.array_equal(Q2, 2 * P)
+    Q2 = np.rint(P * (1 << 20)).astype(np.int64)
+    assert np.array_equal(Q2, P * (1 << 20)) and np.abs(P).max() < 64
     V = np.unique(rep)
     out = []
     for a, b in cons:
