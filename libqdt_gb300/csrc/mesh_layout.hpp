@@ -45,7 +45,7 @@ struct MeshVertex
 {
     double   x, y;
     uint32_t orig;   // point index in the context
-    int      he;     // an outgoing half-edge (the first one in triangle order)
+    int      he;     // an outgoing half-edge (after a build the first one in triangle order)
 };
 
 struct MeshHalfEdge

@@ -206,13 +206,14 @@ QDT_HD inline int orient_v(const MeshVertex* v, int a, int b, int c)
 }
 
 // Traces the segment from mesh vertex u to mesh vertex w (u != w). Visits
-// u's fan in the order of the host's for_each_out (counter-clockwise from
-// u's stored half-edge, then clockwise for a hull vertex): an edge u-w in
-// either direction means kTraceOk with nothing crossed; otherwise the first
-// fan triangle the segment leaves through, or a neighbour on the segment,
-// decides the start, and the march counts the edges crossed until w, a
-// vertex on the segment, or a constrained edge. *crossed = edges crossed
-// before the outcome. Each fan visit and each crossing is one step of cap.
+// u's fan counter-clockwise from u's stored half-edge, then clockwise for a
+// hull vertex: an edge u-w in either direction means kTraceOk with nothing
+// crossed; otherwise the fan triangle the segment leaves through, or a
+// neighbour on the segment, decides the start (at most one of the two
+// exists, so the outcome does not depend on which half-edge u stores), and
+// the march counts the edges crossed until w, a vertex on the segment, or a
+// constrained edge. *crossed = edges crossed before the outcome. Each fan
+// visit and each crossing is one step of cap.
 QDT_HD inline int trace_segment(const MeshVertex* v, const MeshHalfEdge* h, int nv, int nh, int u, int w, int cap,
     int* crossed)
 {
