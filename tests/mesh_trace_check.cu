@@ -1,14 +1,17 @@
-// Host harness of the constraint trace the GPU runs (mesh_walk.cuh,
-// trace_segment; tests/test_trace_host.py). Compiled with nvcc as a host
-// program: the same source the device kernel k_mesh_trace is built from,
-// run here on the CPU. It builds the half-edge mesh of a triangulation the
+// Host harness of the constraint trace and the point location the GPU runs
+// (mesh_walk.cuh: trace_segment, walk and classify; tests/test_trace_host.py).
+// Compiled with nvcc as a host program: the same source the device kernels
+// k_mesh_trace and k_mesh_locate are built from, run here on the CPU. It builds the half-edge mesh of a triangulation the
 // way the mesh builders lay it out (half-edges 3t, 3t+1, 3t+2 of triangle
 // t, each vertex storing its first outgoing half-edge in triangle order),
-// flags the constrained edges it is given, and traces the queried segments.
+// flags the constrained edges it is given, traces the queried segments and
+// locates the queried points (a walk from a given half-edge, then the
+// canonical answer).
 //
 // Input (binary file): int32 nv; float64 xy[2 nv]; int32 ntri;
 // int32 tri[3 ntri]; int32 ncons; int32 cons[2 ncons]; int32 nq;
-// int32 q[2 nq]. Output: one line "status crossed" per query.
+// int32 q[2 nq]; int32 nl; float64 p[2 nl]; int32 start[nl]. Output: one
+// line "status crossed" per segment, then one line "tri where" per point.
 #include <climits>
 #include <cstdio>
 #include <map>
@@ -40,6 +43,11 @@ int main(int argc, char** argv)
     if (!get(f, cons.data(), cons.size()) || !get(f, &nq, 1) || nq < 0) return 3;
     std::vector<int> q(2 * (size_t)nq);
     if (!get(f, q.data(), q.size())) return 3;
+    int nl = 0;
+    if (!get(f, &nl, 1) || nl < 0) return 3;
+    std::vector<double> p(2 * (size_t)nl);
+    std::vector<int>    start(nl);
+    if (!get(f, p.data(), p.size()) || !get(f, start.data(), start.size())) return 3;
     fclose(f);
 
     std::vector<MeshVertex>   v(nv);
@@ -73,6 +81,13 @@ int main(int argc, char** argv)
         int       crossed = 0;
         const int st = trace_segment(v.data(), h.data(), nv, (int)h.size(), q[2 * i], q[2 * i + 1], INT_MAX, &crossed);
         printf("%d %d\n", st, crossed);
+    }
+    const int nh = (int)h.size();
+    for (int i = 0; i < nl; ++i)
+    {
+        LocResult r = walk(v.data(), h.data(), nv, nh, start[i], p[2 * i], p[2 * i + 1], INT_MAX);
+        if (r.where == kLocInside) r = classify(v.data(), h.data(), nv, nh, r.he, p[2 * i], p[2 * i + 1], INT_MAX);
+        printf("%d %d\n", r.where == kLocOutside ? -1 : r.tri, r.where);
     }
     return 0;
 }

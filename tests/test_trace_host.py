@@ -1,14 +1,19 @@
-"""The constraint trace of the GPU path (mesh_walk.cuh, trace_segment, which
-the kernel k_mesh_trace runs for qdtg_trace_constraints) run on the CPU: the
-harness tests/mesh_trace_check.cu is compiled with nvcc as a host program
-from the same source. On triangulations edited by insertions and
-constraints through the library (loaded with the oracle's triangulation,
-no GPU needed), every traced status must equal what qdt_insert_constraint
+"""The constraint trace and the point location of the GPU path
+(mesh_walk.cuh: trace_segment, which the kernel k_mesh_trace runs for
+qdtg_trace_constraints; walk and classify, which k_mesh_locate runs for
+qdtg_locate_points) run on the CPU: the harness tests/mesh_trace_check.cu is
+compiled with nvcc as a host program from the same source. On
+triangulations edited by insertions and constraints through the library
+(loaded with the oracle's triangulation, no GPU needed), every traced status must equal what qdt_insert_constraint
 returns for the same segment on the same state, and for a segment that is
 accepted, the count of crossed edges must equal the edges of the
 triangulation the open segment crosses (counted with the oracle's exact
-orientation). The GPU tests compare the kernel with the same calls on the
-device (tests/test_gpu_trace.py)."""
+orientation). Points located from random start half-edges (at vertices, on
+edges, inside, outside the hull) must get the brute-force answer: the
+smallest triangle that holds the point, border included, and whether it
+lies inside, on an edge or on a vertex. The GPU tests compare the kernels
+with the same calls on the device (tests/test_gpu_trace.py,
+tests/test_gpu_locate.py)."""
 import os
 import shutil
 import subprocess
@@ -71,8 +76,8 @@ def _state(lib, pts, ops, r):
 
 def _constrained_edges(t, ops, st):
     """The accepted constraints as edges now: the pieces a later insertion
-    on a constrained edge split it into (exact: coordinates on a grid of
-    1/2 below 64 in magnitude, or no point on any edge)."""
+    on a constrained edge split it into (exact on a half-integer grid; the
+    uniform doubles put no point on an edge)."""
     rep = t.rep_array()
     P = np.array([t.point(i)[1] for i in range(t.points_size())])
     V = np.unique(rep)
@@ -108,8 +113,18 @@ def _crossed_edges(P, tris, u, w):
     return n
 
 
+def _locate_brute(P, tris, x):
+    """(smallest triangle holding x, border included; 0 inside, 1 on an
+    edge, 2 on a vertex), or (-1, -1) outside the hull."""
+    for k, t3 in enumerate(tris):
+        o = [O.orient2d(P[t3[i]], P[t3[(i + 1) % 3]], x) for i in range(3)]
+        if min(o) >= 0:
+            return k, 3 - sum(1 for s in o if s != 0)
+    return -1, -1
+
+
 @pytest.mark.parametrize("seed", range(12))
-def test_host_trace_equals_insert_constraint(harness, tmp_path, seed):
+def test_trace_and_locate_on_the_cpu(harness, tmp_path, seed):
     lib = G.load()
     pts, ops = _case(seed)
     r = O.triangulate(pts)
@@ -128,17 +143,28 @@ def test_host_trace_equals_insert_constraint(harness, tmp_path, seed):
         u, w = (int(x) for x in rng.choice(used, size=2))
         if u != w:
             qs.append((u, w))
+    # points to locate: vertices, edge midpoints, random points in and around the hull
+    lo, hi = P[used].min(axis=0), P[used].max(axis=0)
+    locs = [P[int(v)] for v in rng.choice(used, size=20)]
+    for t3 in tris[rng.integers(0, len(tris), size=20)]:
+        locs.append((P[t3[0]] + P[t3[1]]) / 2)
+    locs += list(lo - 0.1 * (hi - lo) + rng.random((40, 2)) * 1.2 * (hi - lo))
+    locs = np.array(locs, dtype=np.float64)
+    starts = rng.integers(0, 3 * len(tris), size=len(locs)).astype(np.int32)
     blob = (np.int32(len(P)).tobytes() + P.astype(np.float64).tobytes()
             + np.int32(len(tris)).tobytes() + tris.astype(np.int32).tobytes()
             + np.int32(len(cons)).tobytes() + np.array(cons, dtype=np.int32).reshape(-1, 2).tobytes()
-            + np.int32(len(qs)).tobytes() + np.array(qs, dtype=np.int32).tobytes())
+            + np.int32(len(qs)).tobytes() + np.array(qs, dtype=np.int32).tobytes()
+            + np.int32(len(locs)).tobytes() + locs.tobytes() + starts.tobytes())
     f = tmp_path / "mesh.bin"
     f.write_bytes(blob)
     out = subprocess.run([harness, str(f)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     got = [tuple(int(x) for x in line.split()) for line in out.stdout.split("\n") if line.strip()]
-    assert len(got) == len(qs)
-    for (u, w), (status, crossed) in zip(qs, got):
+    assert len(got) == len(qs) + len(locs)
+    for x, (tri, where) in zip(locs, got[len(qs):]):
+        assert (tri, where) == _locate_brute(P, tris, x), (seed, x)
+    for (u, w), (status, crossed) in zip(qs, got[:len(qs)]):
         assert status in STATUS, (seed, u, w, status)
         t2, _ = _state(lib, pts, ops, r)
         with t2:
