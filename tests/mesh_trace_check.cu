@@ -1,9 +1,10 @@
 // Host harness of the constraint trace and the point location the GPU runs
 // (mesh_walk.cuh: trace_segment, walk and classify; tests/test_trace_host.py).
 // Compiled with nvcc as a host program: the same source the device kernels
-// k_mesh_trace and k_mesh_locate are built from, run here on the CPU. It builds the half-edge mesh of a triangulation the
-// way the mesh builders lay it out (half-edges 3t, 3t+1, 3t+2 of triangle
-// t, each vertex storing its first outgoing half-edge in triangle order),
+// k_mesh_trace and k_mesh_locate are built from, run here on the CPU. It
+// builds the half-edge mesh of a triangulation the way the mesh builders lay
+// it out (half-edges 3t, 3t+1, 3t+2 of triangle t, each vertex storing its
+// first outgoing half-edge in triangle order),
 // flags the constrained edges it is given, traces the queried segments and
 // locates the queried points (a walk from a given half-edge, then the
 // canonical answer).
