@@ -165,3 +165,25 @@ def test_set_triangulation_checks(lib):
         bad = pts.copy()
         bad[2, 0] = np.nan
         assert t.set_triangulation(bad, np.array([[0, 1, 2]]), np.array([0, 1, 2, 1])) == Q.QDT_ERR_NOT_FINITE
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_batch_insertion_equals_sequential_on_host(lib, seed):
+    """qdtg_insert_points without a GPU (each walk starts from the host's own
+    seeds instead of a device location) gives what qdt_insert_point gives
+    point by point: statuses, indices, triangles and representatives."""
+    rng = np.random.default_rng(60 + seed)
+    if seed % 2:
+        pts = rng.integers(0, 20, size=(300, 2)).astype(np.float64)
+        q = rng.integers(-2, 22, size=(200, 2)) + 0.5 * rng.integers(0, 2, size=(200, 2))
+    else:
+        pts = rng.random((400, 2))
+        q = rng.random((200, 2)) * 1.3 - 0.15
+    with loaded(lib, pts) as a, loaded(lib, pts) as b:
+        st, res, idx = a.insert_points(q)
+        assert st == Q.QDT_OK
+        seq = [b.insert_point(float(x), float(y)) for x, y in q]
+        assert [int(v) for v in res] == [s for s, _ in seq]
+        assert [int(v) for v in idx] == [i for _, i in seq]
+        assert np.array_equal(O.canonical(a.triangles_array()), O.canonical(b.triangles_array()))
+        assert np.array_equal(a.rep_array(), b.rep_array())
