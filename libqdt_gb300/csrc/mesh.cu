@@ -59,6 +59,44 @@ struct SeedGrid
     size_t           walked = 0;   // walk steps taken before the grid existed
 };
 
+// Directed edges of one edit looked up by their end points: open addressing
+// with linear probing, at most half full, its storage kept from edit to
+// edit.
+struct EdgeTable
+{
+    static constexpr uint64_t kEmpty = ~0ull;   // no edge key: vertex ids are below 2^31
+    std::vector<uint64_t>     key;
+    std::vector<int>          val;
+    int                       shift = 64;
+
+    void reset(size_t n)
+    {
+        int bits = 4;
+        while (((size_t)1 << bits) < 2 * n) ++bits;
+        key.assign((size_t)1 << bits, kEmpty);
+        val.resize((size_t)1 << bits);
+        shift = 64 - bits;
+    }
+    size_t home(uint64_t k) const { return (size_t)((k * 0x9E3779B97F4A7C15ull) >> shift); }
+    void   put(uint64_t k, int v)
+    {
+        const size_t m = key.size() - 1;
+        size_t       i = home(k);
+        while (key[i] != kEmpty && key[i] != k) i = (i + 1) & m;
+        key[i] = k;
+        val[i] = v;
+    }
+    int get(uint64_t k) const   // -1 when absent
+    {
+        const size_t m = key.size() - 1;
+        for (size_t i = home(k);; i = (i + 1) & m)
+        {
+            if (key[i] == k) return val[i];
+            if (key[i] == kEmpty) return -1;
+        }
+    }
+};
+
 struct Mesh
 {
     MeshVec<MV>           v;
@@ -71,6 +109,7 @@ struct Mesh
     int                   last = 0;   // a half-edge near the last edit: the next walk's default start
     uint64_t              id = next_id();   // identifies this mesh to the device mirror
     uint64_t              version = 0;      // bumped by every call that may change the mesh
+    EdgeTable             fresh_edges, outer_edges;   // scratch of the constraint fill
 
     static uint64_t next_id()
     {
@@ -862,54 +901,62 @@ int fill_channel(Context& c, Mesh& M, int u, int w, const Channel& ch)
             outer.push_back(Outer{ edge_key(M.h[e].org, dst(M, e)), tw, M.h[e].cons });
         }
     }
-    std::sort(outer.begin(), outer.end(), [](const Outer& x, const Outer& y) { return x.key < y.key; });
+    EdgeTable& ot = M.outer_edges;
+    ot.reset(outer.size());
+    for (size_t i = 0; i < outer.size(); ++i) ot.put(outer[i].key, (int)i);
 
     Reuse r;
     reuse_triangles(M, ch.tris, r);
-    std::vector<std::pair<uint64_t, int>> fresh;   // (key of a -> b, half-edge)
-    for (const Tri3& q : made)
+    EdgeTable& ft = M.fresh_edges;   // key of a -> b: its new half-edge
+    ft.reset(3 * made.size());
+    std::vector<int> made_he(3 * made.size());
+    for (size_t i = 0; i < made.size(); ++i)
     {
+        const Tri3&  q = made[i];
         const size_t t = r.slot(c);
         const int    e0 = r.he(M), e1 = r.he(M), e2 = r.he(M);
         put_triangle(c, M, t, e0, e1, e2, q.a, q.b, q.c);
         const int v3[3] = { q.a, q.b, q.c }, e3[3] = { e0, e1, e2 };
         for (int k = 0; k < 3; ++k)
         {
-            fresh.emplace_back(edge_key(v3[k], v3[(k + 1) % 3]), e3[k]);
+            ft.put(edge_key(v3[k], v3[(k + 1) % 3]), e3[k]);
+            made_he[3 * i + k] = e3[k];
             M.h[e3[k]].twin = -1;
             M.h[e3[k]].cons = 0;
             M.v[v3[k]].he = e3[k];
         }
     }
     if (!r.all_used()) return QDT_ERR_INTERNAL;
-    std::sort(fresh.begin(), fresh.end());
-    for (const auto& f : fresh)
+    for (size_t i = 0; i < made.size(); ++i)
     {
-        const uint32_t a = (uint32_t)(f.first >> 32), b = (uint32_t)f.first;
-        const uint64_t rev = edge_key((int)b, (int)a);
-        const auto     in = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(rev, INT_MIN));
-        if (in != fresh.end() && in->first == rev)
+        const int v3[3] = { made[i].a, made[i].b, made[i].c };
+        for (int k = 0; k < 3; ++k)
         {
-            M.h[f.second].twin = in->second;   // a diagonal, or the new edge u-w
-            continue;
+            const int a = v3[k], b = v3[(k + 1) % 3];
+            const int e = made_he[3 * i + k];
+            const int in = ft.get(edge_key(b, a));
+            if (in >= 0)
+            {
+                M.h[e].twin = in;   // a diagonal, or the new edge u-w
+                continue;
+            }
+            const int o = ot.get(edge_key(a, b));
+            if (o < 0) return QDT_ERR_INTERNAL;
+            M.h[e].twin = outer[o].ext;
+            M.h[e].cons = outer[o].cons;
+            if (outer[o].ext >= 0) M.h[outer[o].ext].twin = e;
         }
-        const auto o = std::lower_bound(outer.begin(), outer.end(), f.first,
-            [](const Outer& x, uint64_t k) { return x.key < k; });
-        if (o == outer.end() || o->key != f.first) return QDT_ERR_INTERNAL;
-        M.h[f.second].twin = o->ext;
-        M.h[f.second].cons = o->cons;
-        if (o->ext >= 0) M.h[o->ext].twin = f.second;
     }
     for (const uint64_t k : antennas)
     {
-        const auto f = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(k, INT_MIN));
-        if (f == fresh.end() || f->first != k) return QDT_ERR_INTERNAL;
-        set_constrained(M, f->second);
+        const int e = ft.get(k);
+        if (e < 0) return QDT_ERR_INTERNAL;
+        set_constrained(M, e);
     }
-    const auto uw = std::lower_bound(fresh.begin(), fresh.end(), std::make_pair(edge_key(u, w), INT_MIN));
-    if (uw == fresh.end() || uw->first != edge_key(u, w)) return QDT_ERR_INTERNAL;
-    set_constrained(M, uw->second);
-    M.last = uw->second;
+    const int uw = ft.get(edge_key(u, w));
+    if (uw < 0) return QDT_ERR_INTERNAL;
+    set_constrained(M, uw);
+    M.last = uw;
     return QDT_OK;
 }
 
