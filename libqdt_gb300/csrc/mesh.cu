@@ -841,15 +841,24 @@ bool fill_polygon(const Mesh& M, int a, int b, const std::vector<int>& poly, std
         int    a, b;
         size_t lo, hi;
     };
+    // the polygon's coordinates side by side, as the scans read them
+    std::vector<double> px(poly.size()), py(poly.size());
+    for (size_t i = 0; i < poly.size(); ++i)
+    {
+        px[i] = M.v[poly[i]].x;
+        py[i] = M.v[poly[i]].y;
+    }
     std::vector<Part> todo{ Part{ a, b, 0, poly.size() } };
     while (!todo.empty())
     {
         const Part q = todo.back();
         todo.pop_back();
         if (q.lo >= q.hi) continue;
-        size_t best = q.lo;
+        const MV& A = M.v[q.a];
+        const MV& B = M.v[q.b];
+        size_t    best = q.lo;
         for (size_t i = q.lo + 1; i < q.hi; ++i)
-            if (circle4(M, q.a, q.b, poly[best], poly[i]) > 0) best = i;
+            if (incircle_sign(A.x, A.y, B.x, B.y, px[best], py[best], px[i], py[i]) > 0) best = i;
         const int c = poly[best];
         if (orient3(M, q.a, q.b, c) <= 0) return false;
         out.push_back(Tri3{ q.a, q.b, c });
