@@ -155,36 +155,32 @@ inline int circle_holds(const Mesh& M, int t, double px, double py)
     return incircle_sign(A.x, A.y, B.x, B.y, C.x, C.y, px, py);
 }
 
-// Visits the outgoing half-edges of vertex x, one per triangle around it,
-// counter-clockwise; around a hull vertex the visit starts at the clockwise-
-// most one, so the open fan is covered once. f returns true to stop; the
-// result says whether it did.
+// Visits the outgoing half-edges of vertex x, one per triangle around it:
+// counter-clockwise from the stored one until the fan closes, and around a
+// hull vertex then clockwise from the stored one to the hull. f returns true
+// to stop; the result says whether it did.
 template <class F>
 bool around(const Mesh& M, int x, F&& f)
 {
-    int s = M.v[x].he;
+    const int s = M.v[x].he;
     if (s < 0) return false;
     const size_t cap = M.h.size() + 1;
     size_t       n = 0;
-    // clockwise neighbour of k: the half-edge after its twin
-    for (int k = s;;)
-    {
-        const int t = M.h[k].twin;
-        if (t < 0)
-        {
-            s = k;
-            break;
-        }
-        k = M.h[t].next;
-        if (k == s || ++n > cap) break;
-    }
-    n = 0;
     for (int k = s;;)
     {
         if (f(k)) return true;
         const int t = M.h[prv(M, k)].twin;   // counter-clockwise neighbour
-        if (t < 0 || t == s || ++n > cap) return false;
+        if (t == s) return false;            // the fan closed: all visited
+        if (t < 0 || ++n > cap) break;
         k = t;
+    }
+    for (int k = s;;)
+    {
+        const int t = M.h[k].twin;   // clockwise neighbour: the half-edge after the twin
+        if (t < 0) return false;
+        k = M.h[t].next;
+        if (k == s || ++n > cap) return false;
+        if (f(k)) return true;
     }
 }
 
