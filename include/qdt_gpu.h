@@ -263,9 +263,12 @@ QDT_API size_t qdtg_copy_rep(const qdt_t* ptr, uint32_t* out, size_t cap);
    (QDT_ERR_NULL_ARGUMENT); a NaN or infinite coordinate
    (QDT_ERR_NOT_FINITE); a representative that is not the lowest index of
    equal coordinates, a triangle corner out of range or not its own
-   representative, a triangle not strictly counter-clockwise, or a directed
-   edge used twice (QDT_ERR_INVALID_INDEX). Any rejection leaves the
-   context empty. */
+   representative, a triangle not strictly counter-clockwise, a directed
+   edge used twice, or triangles that do not cover the convex hull of the
+   distinct points once (a distinct point that is no corner, a boundary
+   that is not one cycle turning left or running straight at every corner,
+   or a region covered twice) (QDT_ERR_INVALID_INDEX). Any rejection leaves
+   the context empty. */
 QDT_API qdt_status qdtg_set_triangulation(qdt_t* ptr, const qdt_vec2d* pts, size_t n, const uint32_t* rep,
     const uint32_t* tris, size_t ntri);
 

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <iterator>
 #include <new>
 #include <vector>
 
@@ -770,6 +771,51 @@ QDT_API qdt_status qdtg_set_triangulation(qdt_t* ptr, const qdt_vec2d* pts, size
         }
         std::sort(edges.begin(), edges.end());
         if (std::adjacent_find(edges.begin(), edges.end()) != edges.end()) return QDT_ERR_INVALID_INDEX;
+        // the triangles cover the convex hull of the distinct points once:
+        // every distinct point is a corner; the edges without a reverse form
+        // one cycle that turns left or runs straight at every corner; and the
+        // triangles' areas add up to the area inside it (not twice as much)
+        if (ntri)
+        {
+            std::vector<uint8_t> corner(n, 0);
+            for (size_t i = 0; i < 3 * ntri; ++i) corner[tris[i]] = 1;
+            for (size_t i = 0; i < n; ++i)
+                if ((rep ? rep[i] : i) == i && !corner[i]) return QDT_ERR_INVALID_INDEX;
+            std::vector<uint64_t> rev(edges.size());
+            for (size_t i = 0; i < edges.size(); ++i) rev[i] = (edges[i] << 32) | (edges[i] >> 32);
+            std::sort(rev.begin(), rev.end());
+            std::vector<uint64_t> hull;   // a -> b with no b -> a, sorted by a
+            std::set_difference(edges.begin(), edges.end(), rev.begin(), rev.end(), std::back_inserter(hull));
+            for (size_t i = 1; i < hull.size(); ++i)
+                if ((hull[i] >> 32) == (hull[i - 1] >> 32)) return QDT_ERR_INVALID_INDEX;
+            auto after = [&](uint32_t a) -> int64_t {
+                const auto it = std::lower_bound(hull.begin(), hull.end(), (uint64_t)a << 32);
+                return (it != hull.end() && (*it >> 32) == a) ? (int64_t)(uint32_t)*it : -1;
+            };
+            if (hull.empty()) return QDT_ERR_INVALID_INDEX;
+            const uint32_t first = (uint32_t)(hull[0] >> 32);
+            const double   ox = pts[first].x, oy = pts[first].y;
+            double         inside = 0.0, covered = 0.0;   // twice the areas
+            size_t         steps = 0;
+            for (uint32_t a = first;;)
+            {
+                const int64_t b = after(a);
+                const int64_t d = b < 0 ? -1 : after((uint32_t)b);
+                if (d < 0 || ++steps > hull.size()) return QDT_ERR_INVALID_INDEX;
+                const qdt_vec2d &A = pts[a], &B = pts[b], &D = pts[d];
+                if (qdtg::orient2d_sign(A.x, A.y, B.x, B.y, D.x, D.y) < 0) return QDT_ERR_INVALID_INDEX;
+                inside += (A.x - ox) * (B.y - oy) - (B.x - ox) * (A.y - oy);
+                a = (uint32_t)b;
+                if (a == first) break;
+            }
+            if (steps != hull.size()) return QDT_ERR_INVALID_INDEX;   // more than one cycle
+            for (size_t t = 0; t < ntri; ++t)
+            {
+                const qdt_vec2d &a = pts[tris[3 * t]], &b = pts[tris[3 * t + 1]], &d = pts[tris[3 * t + 2]];
+                covered += (b.x - a.x) * (d.y - a.y) - (b.y - a.y) * (d.x - a.x);
+            }
+            if (covered > 1.5 * inside) return QDT_ERR_INVALID_INDEX;   // a region covered twice
+        }
         c->points.resize(2 * n);
         for (size_t i = 0; i < n; ++i)
         {

@@ -165,6 +165,19 @@ def test_set_triangulation_checks(lib):
         bad = pts.copy()
         bad[2, 0] = np.nan
         assert t.set_triangulation(bad, np.array([[0, 1, 2]]), np.array([0, 1, 2, 1])) == Q.QDT_ERR_NOT_FINITE
+    # the triangles must cover the convex hull of the distinct points once
+    sq = np.array([[0.0, 0.0], [2.0, 0.0], [2.0, 2.0], [0.0, 2.0], [1.0, 1.0]])
+    fan = np.array([[0, 1, 4], [1, 2, 4], [2, 3, 4], [3, 0, 4]])
+    with G.Triangulation(lib) as t:
+        assert t.set_triangulation(sq, fan) == Q.QDT_OK
+        assert t.set_triangulation(sq, fan[:3]) == Q.QDT_ERR_INVALID_INDEX         # a reflex corner at (1,1)
+        assert t.set_triangulation(sq, fan[[0, 2]]) == Q.QDT_ERR_INVALID_INDEX     # two pieces
+        assert t.set_triangulation(sq, np.array([[0, 1, 2], [0, 2, 3]])) == Q.QDT_ERR_INVALID_INDEX   # (1,1) unused
+        ring = np.array([[0.0, 0.0], [6.0, 0.0], [6.0, 6.0], [0.0, 6.0], [2.0, 2.0], [4.0, 2.0], [4.0, 4.0],
+                         [2.0, 4.0]])
+        holed = np.array([[0, 1, 5], [0, 5, 4], [1, 2, 6], [1, 6, 5], [2, 3, 7], [2, 7, 6], [3, 0, 4], [3, 4, 7]])
+        assert t.set_triangulation(ring, holed) == Q.QDT_ERR_INVALID_INDEX        # a hole in the middle
+        assert t.set_triangulation(ring, np.concatenate([holed, [[4, 5, 6], [4, 6, 7]]])) == Q.QDT_OK
 
 
 @pytest.mark.parametrize("seed", range(4))
