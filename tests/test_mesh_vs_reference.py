@@ -4,12 +4,16 @@ itself, on operation sequences that are not in the committed fixtures.
 Where the reference was compiled from its own sources into oracle/_ref, each
 case triangulates fresh seeded points in both libraries (ours is loaded with
 the oracle's triangulation through qdtg_set_triangulation, so no GPU is
-needed), applies the same insertions and constraints in the same order, then one
-qdt_insert_constraints_batch call, and requires equal statuses, returned indices, used flags and triangle counts;
-equal triangle sets where the input is in general position (the constrained
-Delaunay triangulation is unique there), and everywhere a valid constrained
-Delaunay triangulation that holds every accepted constraint (as the pieces
-later insertions on it split it into). Skipped where the reference is not compiled.
+needed), applies the same insertions and constraints in the same order,
+then one qdt_insert_constraints_batch call. Inputs: uniform points; integer
+points with duplicates and insertions on vertices, edges and outside the
+hull; a few integer points with insertions at midpoints; coordinates from
+2^-100 to 2^100. Required: equal statuses, returned indices, used flags
+and triangle counts; equal triangle sets where the input is in general
+position (the constrained Delaunay triangulation is unique there); and
+everywhere a valid constrained Delaunay triangulation that holds every
+accepted constraint (as the pieces later insertions on it split it into).
+Skipped where the reference is not compiled.
 """
 import os
 
@@ -36,9 +40,20 @@ def libs():
 def _case(seed):
     """(points, ops, general position) for one seed."""
     rng = np.random.default_rng(seed)
-    kind = seed % 5
+    kind = seed % 6
     n = int(rng.integers(3, 400))
     ops = []
+    if kind == 5:      # coordinates from 2^-100 to 2^100 in one set, insertions alike
+        def draw(k):
+            return (rng.random((k, 2)) * 2 - 1) * np.ldexp(1.0, rng.integers(-100, 100, size=(k, 2)))
+        p = draw(n)
+        for _ in range(int(rng.integers(1, 60))):
+            if rng.random() < 0.6:
+                q = draw(1)[0]
+                ops.append(("insert", float(q[0]), float(q[1])))
+            else:
+                ops.append(("constraint", int(rng.integers(0, n + 3)), int(rng.integers(0, n + 3))))
+        return p, ops, True
     if kind == 4:      # a few integer points; insertions at midpoints of point pairs, repeats, far points
         p = rng.integers(0, int(rng.integers(2, 17)), size=(int(rng.integers(3, 12)), 2)).astype(np.float64)
         allp = [tuple(x) for x in p]
