@@ -225,3 +225,35 @@ def test_mesh_built_on_gpu_equals_host(lib):
         assert results[0][0] == results[1][0], i
         assert results[0][2] == results[1][2], i
         assert np.array_equal(results[0][1], results[1][1]), i
+
+
+# Small edits around constrained hull edges and enclosed fans, after a batch
+# call on the GPU: the statuses (and triangle counts) the reference library
+# returns for the same calls, serial and parallel alike.
+_EDIT_CASES = [
+    # a point on a constrained hull edge splits it; a point below sees both halves
+    ("split_hull", [[0, 0], [4, 0], [4, 4], [0, 4], [2, 2.5]],
+     [("constraint", 0, 1), ("insert", 2.0, 0.0), ("insert", 2.0, -3.0), ("constraint", 6, 2),
+      ("constraint", 6, 3), ("constraint", 6, 4)], [0, 0, 5, 0, 6, -8, -8, -9], 7),
+    # a segment crossing the whole fan of (0, 3.5) keeps the constrained edge to (0, 0)
+    ("antenna", [[0, 0], [-5, 10], [5, 10], [0, 3.5], [-20, 4], [20, 4], [0, -6], [0, 16]],
+     [("constraint", 0, 3), ("constraint", 4, 5), ("insert", -1.0, 1.0), ("insert", 1.0, 2.0),
+      ("constraint", 8, 9)], [0, 0, 0, 8, 0, 9, -8], 14),
+    # a point outside the hull, then a constraint from the end of the open border
+    ("open_border", [[3, 8], [5, 3], [1, 1], [6, 9], [8, 1], [7, 2], [3, 8], [8, 0]],
+     [("insert", 0.0, 6.0), ("constraint", 6, 5)], [0, 8, 0], 8),
+    # a constrained hull edge hides the triangle behind it from a point outside
+    ("hidden_hull", [[0, 0], [4, 0], [4, 4], [0, 4], [2, 1]],
+     [("constraint", 0, 1), ("insert", 2.0, -1.0), ("constraint", 5, 4), ("constraint", 5, 2)],
+     [0, 0, 5, -8, -8], 5),
+]
+
+
+@pytest.mark.parametrize("case", _EDIT_CASES, ids=[c[0] for c in _EDIT_CASES])
+def test_edits_at_constrained_hull_edges(lib, case):
+    name, pts, ops, want, ntri = case
+    for par in (False, True):
+        t, st = run_ops(lib, np.array(pts, dtype=np.float64), ops, par)
+        with t:
+            assert st.tolist() == want, (name, par, st)
+            assert t.triangles_size() == ntri, name
